@@ -1,0 +1,196 @@
+// Finaliser, launch dispatch and debug kernels.
+#include "hexo_device.cuh"
+#include "hexo_final.h"
+#include "hexo_launch.h"
+
+namespace hexo {
+
+cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t smem, cudaStream_t st,
+                         const KernelArgs &a) {
+    const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll);
+    if (fn == nullptr) return cudaErrorInvalidValue;
+    KernelArgs args = a;
+    void *params[] = {&args};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(sh.block), params, smem, st);
+}
+
+__global__ void finalize_kernel(const unsigned long long *__restrict__ acc, const uint64_t *__restrict__ n_paths,
+                                const double *__restrict__ disc, uint32_t n, double *__restrict__ price,
+                                double *__restrict__ se) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t l[kLimbs];
+#pragma unroll
+    for (int x = 0; x < kLimbs; ++x) l[x] = acc[(size_t)i * kLimbs + x];
+    double p, s;
+    finalize_limbs6(l, n_paths[i], disc[i], &p, &s);
+    price[i] = p;
+    se[i] = s;
+}
+
+cudaError_t launch_finalize(const unsigned long long *acc, const uint64_t *n_paths, const double *disc, uint32_t n,
+                            double *price, double *se, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_paths, disc, n, price, se);
+    return cudaGetLastError();
+}
+
+// Raw stream words: block 0 is the state after initialisation with its
+// lanes reversed, then one block per round.
+__global__ void dbg_words_kernel(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_streams) return;
+    dev::Shishua g;
+    dev::sh_init(g, (uint64_t)(uint32_t)(seed + k));
+    uint64_t o[16];
+#pragma unroll
+    for (int L = 0; L < 4; ++L)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[4 * L + q] = g.s[4 * (3 - L) + q];
+    for (uint32_t w = 0; w < n_words; w += 16) {
+        if (w > 0) dev::sh_round(g, o);
+#pragma unroll
+        for (int q = 0; q < 16; ++q)
+            if (w + q < n_words) out[(size_t)k * n_words + w + q] = o[q];
+    }
+}
+
+// The two-buffer RNG through the same ring code as the path kernel.
+__global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t *ring = reinterpret_cast<uint64_t *>(smem_raw);
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t bd = blockDim.x;
+    uint64_t *base = ring + threadIdx.x;
+    dev::Shishua g;
+    dev::RngCursor c;
+    dev::rng_start(g, c, base, bd, seed + k);
+    for (uint32_t i = 0; i < n; i += 2) {
+        dev::rng_topup(g, c, base, bd);   // same cadence as one QE step (two draws)
+        for (uint32_t h = i; h < i + 2 && h < n; ++h) {
+            double v;
+            if (kinds[h]) v = dev::uniform_f64(dev::rng_next_u(g, c, base, bd));
+            else v = (double)dev::as241_word(dev::rng_next_g(g, c, base, bd));
+            if (k < n_streams) out[(size_t)k * n + h] = v;
+        }
+    }
+}
+
+__global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)dev::as241_word(words[i]);
+}
+
+cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st) {
+    dbg_words_kernel<<<(n_streams + 127) / 128, 128, 0, st>>>(seed, n_streams, n_words, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
+                             cudaStream_t st) {
+    const uint32_t bd = 64;
+    const size_t smem = (size_t)kRingSlots * kRngWords * bd * sizeof(uint64_t);
+    dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, n_streams, kinds, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dbg_normals(const uint64_t *words, uint64_t n, double *out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dbg_normals_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(words, n, out);
+    return cudaGetLastError();
+}
+
+} // namespace hexo
+
+namespace hexo {
+
+// ------------------------------------------------------ pipe peak probes
+// Eight independent dependency chains per thread keep each pipe busy; the
+// result is written only if it is impossible, so the work is not removed.
+
+__global__ void peak_ffma_kernel(int iters, float *sink) {
+    float a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = 1.0f + 1e-3f * (threadIdx.x + j);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = fmaf(a[j], 0.9999f, 1e-4f);
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += a[j];
+    if (s == -1.0f) sink[0] = s;
+}
+
+__global__ void peak_dfma_kernel(int iters, double *sink) {
+    double a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = 1.0 + 1e-3 * (threadIdx.x + j);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = fma(a[j], 0.9999, 1e-4);
+    double s = 0.;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += a[j];
+    if (s == -1.0) sink[0] = s;
+}
+
+__global__ void peak_mufu_kernel(int iters, float *sink) {
+    float a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = 0.5f + 1e-3f * (threadIdx.x + j);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(a[j]));
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += a[j];
+    if (s == -1.0f) sink[0] = s;
+}
+
+__global__ void peak_int_kernel(int iters, unsigned *sink) {
+    unsigned a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 2654435761u + j;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = a[j] * 1664525u + 1013904223u;
+    unsigned s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s ^= a[j];
+    if (s == 0xFFFFFFFFu) sink[0] = s;
+}
+
+// Lane operations per second for {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD}.
+cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4) {
+    void *sink = nullptr;
+    cudaError_t e = cudaMalloc(&sink, 64);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int threads = 256, blocks = sm_count * 8;
+    const int iters[4] = {4096, 256, 1024, 4096};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {   // first launch warms up
+            cudaEventRecord(a, st);
+            switch (k) {
+            case 0: peak_ffma_kernel<<<blocks, threads, 0, st>>>(iters[k], (float *)sink); break;
+            case 1: peak_dfma_kernel<<<blocks, threads, 0, st>>>(iters[k], (double *)sink); break;
+            case 2: peak_mufu_kernel<<<blocks, threads, 0, st>>>(iters[k], (float *)sink); break;
+            case 3: peak_int_kernel<<<blocks, threads, 0, st>>>(iters[k], (unsigned *)sink); break;
+            }
+            cudaEventRecord(b, st);
+            e = cudaEventSynchronize(b);
+            if (e != cudaSuccess) break;
+            cudaEventElapsedTime(&ms, a, b);
+        }
+        out4[k] = (double)blocks * threads * iters[k] * 8.0 / (ms * 1e-3);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    return e;
+}
+
+} // namespace hexo

@@ -1,0 +1,53 @@
+// Price and standard error from exact limb sums.  Compiled both for the
+// host (hexo_finalize_limbs, shard merges) and the device (finaliser
+// kernel) with the same unfused IEEE operation sequence, so both produce
+// identical bits.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define HEXO_HD __host__ __device__ __forceinline__
+#else
+#define HEXO_HD inline
+#endif
+
+namespace hexo {
+
+#if defined(__CUDA_ARCH__)
+HEXO_HD double fadd(double a, double b) { return __dadd_rn(a, b); }
+HEXO_HD double fsub(double a, double b) { return __dsub_rn(a, b); }
+HEXO_HD double fmul(double a, double b) { return __dmul_rn(a, b); }
+HEXO_HD double fdiv(double a, double b) { return __ddiv_rn(a, b); }
+HEXO_HD double fsqr(double a) { return __dsqrt_rn(a); }
+HEXO_HD double u64d(uint64_t a) { return __ull2double_rn(a); }
+#else
+HEXO_HD double fadd(double a, double b) { volatile double r = a + b; return r; }
+HEXO_HD double fsub(double a, double b) { volatile double r = a - b; return r; }
+HEXO_HD double fmul(double a, double b) { volatile double r = a * b; return r; }
+HEXO_HD double fdiv(double a, double b) { volatile double r = a / b; return r; }
+HEXO_HD double fsqr(double a) { return sqrt(a); }
+HEXO_HD double u64d(uint64_t a) { return (double)a; }
+#endif
+
+// sum = l[0] + l[1] 2^25 + l[2] 2^50 (exact, 128-bit) converted to double.
+HEXO_HD double limbs_to_double(uint64_t l0, uint64_t l1, uint64_t l2) {
+    const unsigned __int128 s = (unsigned __int128)l0 + ((unsigned __int128)l1 << 25) + ((unsigned __int128)l2 << 50);
+    const uint64_t hi = (uint64_t)(s >> 64), lo = (uint64_t)s;
+    return fadd(fmul(u64d(hi), 18446744073709551616.0), u64d(lo));
+}
+
+HEXO_HD void finalize_limbs6(const uint64_t *l, uint64_t n_paths, double disc, double *price, double *se) {
+    const double n = u64d(n_paths);
+    const double s1 = limbs_to_double(l[0], l[1], l[2]);
+    const double s2 = limbs_to_double(l[3], l[4], l[5]);
+    const double mean = fdiv(fmul(s1, 0x1p-40), n);
+    const double m2 = fdiv(fmul(s2, 0x1p-24), n);
+    double var = 0.0;
+    if (n_paths > 1) var = fmul(fsub(m2, fmul(mean, mean)), fdiv(n, fsub(n, 1.0)));
+    if (!(var > 0.0)) var = 0.0;
+    *price = fmul(disc, mean);
+    *se = fmul(disc, fsqr(fdiv(var, n)));
+}
+
+} // namespace hexo

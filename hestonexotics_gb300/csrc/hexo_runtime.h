@@ -1,0 +1,77 @@
+// Runtime objects behind the opaque handles of hexo_mc.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "hexo_mc.h"
+#include "hexo_plan.h"
+
+namespace hexo {
+
+// A device allocation freed on scope exit.
+struct DevBuf {
+    void *p = nullptr;
+    cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 1); }
+    ~DevBuf() { if (p) cudaFree(p); }
+};
+
+// Planned batch resident on the device, with pinned host mirrors of its outputs.
+struct DeviceBatch {
+    hexo_ctx *ctx = nullptr;
+    BatchPlan plan;
+    bool f32 = false;
+    size_t smem = 0;
+    uint32_t ctas_per_sm = 0, grid = 0;
+    void *dmem = nullptr;
+    size_t bytes = 0;
+    void *hmem = nullptr;
+    KernelArgs args{};
+    uint64_t *d_paths = nullptr;
+    double *d_disc = nullptr, *d_price = nullptr, *d_se = nullptr;
+    double *h_price = nullptr, *h_se = nullptr;
+    unsigned long long *h_acc = nullptr;
+    uint32_t *h_ctl = nullptr;   // queue head, error flags
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around the path kernel
+    uint64_t h2d_bytes = 0;
+    DeviceBatch() = default;
+    DeviceBatch(const DeviceBatch &) = delete;
+    DeviceBatch &operator=(const DeviceBatch &) = delete;
+    ~DeviceBatch();
+};
+
+} // namespace hexo
+
+struct hexo_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t sm_count = 0;
+    size_t smem_optin = 0;
+    uint64_t mem_cap = 0;
+    std::string tune_cache;
+    hexo::LaunchShape shape_f64, shape_f32;   // tuned or default launch shapes
+    std::mutex run_mu;                        // one launch sequence at a time on the stream
+    std::mutex err_mu;
+    std::string last_error;
+};
+
+struct hexo_batch {
+    hexo::DeviceBatch db;
+    std::vector<hexo_request> reqs;
+};
+
+namespace hexo {
+hexo_status ctx_fail(hexo_ctx *ctx, hexo_status s, const std::string &msg);
+hexo_status cuda_fail(hexo_ctx *ctx, cudaError_t e, const char *what);
+LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg);
+hexo_status shape_check(hexo_ctx *ctx, bool f32, const LaunchShape &sh, size_t &smem, uint32_t &ctas_per_sm);
+hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch &db);
+cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc);
+hexo_status batch_wait(DeviceBatch &db);
+hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg &cfg,
+                          uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans);
+void scatter_outputs(const DeviceBatch &db, const hexo_request *reqs, uint32_t n_reqs);
+// Autotune cache: reads ctx->tune_cache (if any) into the context's shapes.
+void tune_load(hexo_ctx *ctx);
+} // namespace hexo

@@ -1,0 +1,93 @@
+// Plain descriptors shared by the host planner and the device kernels.
+//
+// A batch is a set of parameter sets ("sets"), each with its options grouped
+// by distinct maturity ("mats") and a step schedule ("segs").  The schedule
+// is the reference's own time stepping (HSimulation.tpp:29-46 with
+// AsianContract.h:35-38): maturity i is approached with width T_i/steps_i,
+// time accumulates as t += width in double, a maturity is priced after the
+// first step whose time reaches it.  Because that time grid does not depend on
+// the path, the host walks it once per set; a segment is a run of equal-width
+// steps whose last step prices one or more maturities.  Tiles are
+// (set, path block) work items for the persistent kernel.
+#pragma once
+#include <stdint.h>
+
+namespace hexo {
+
+constexpr int kLimbs = 6;            // 3 x 25-bit limbs of sum(pay*2^40), 3 of sum(pay^2*2^24)
+constexpr int kLimbBits = 25;        // a warp adds up to 128 limb values in 32 bits
+constexpr uint32_t kLimbMask = (1u << kLimbBits) - 1u;
+constexpr int kRngWords = 16;        // words per RNG buffer (one SHISHUA block)
+constexpr int kRingSlots = 3;        // per path: normal buffer, uniform buffer, one look-ahead block
+
+struct SegDesc {
+    // FP64 constants of one step width dt (HSimulation.tpp:55-79, hoisted)
+    double dt;      // step width
+    double disc;    // exp(-kappa dt)
+    double cA;      // sigma^2 disc / kappa (1 - disc)
+    double cB;      // theta sigma^2 / (2 kappa) (1 - disc)^2
+    double K0, K1, K2, K3, K4;  // K0 includes (r - q) dt
+    double hdt;       // 0.5 dt: trapezoid weight after a non-pricing step
+    double hdt_after; // 0.5 dt of the next segment: trapezoid weight after the pricing step
+    // FP32 copies
+    float f_disc, f_cA, f_cB, f_K0, f_K1, f_K2, f_K3, f_K4, f_hdt, f_hdt_after;
+    uint32_t n_steps;   // steps in this segment, the last one prices
+    uint32_t mat_begin; // maturities priced after the last step: [mat_begin, mat_end) (set-local)
+    uint32_t mat_end;
+    uint32_t pad;
+};
+
+struct MatDesc {
+    double T;       // maturity
+    double tmtp;    // T - t_prev of the pricing step (AsianContract.h:30-31)
+    double dt;      // T / steps at pricing time (the contract's init_step_size)
+    float f_w;      // tmtp / dt
+    float f_invT;   // 1 / T
+    uint32_t opt_begin, opt_end;   // set-local option range (options sorted by maturity)
+};
+
+struct OptDesc {
+    double strike;
+    float f_strike;
+    uint32_t kind;       // 0 Asian, 1 European
+    uint64_t n_paths;    // paths k < n_paths price this option
+    uint32_t out_index;  // position in the batch's result arrays
+    uint32_t pad;
+};
+
+struct SetDesc {
+    double S0, logS0, v0, theta;
+    float f_S0, f_v0, f_theta, f_pad;
+    uint32_t seed;
+    uint32_t seg_begin, seg_count;
+    uint32_t mat_begin, mat_count;
+    uint32_t opt_begin, opt_count;
+    uint32_t pad;
+    uint64_t n_paths;    // max over options
+};
+
+struct TileDesc {
+    uint64_t path_begin; // first path of the block
+    uint32_t set;        // set index
+    uint32_t seg_count;  // segments this block must run (to its last maturity)
+};
+
+struct KernelArgs {
+    const SetDesc *sets;
+    const SegDesc *segs;     // global arrays; set-local indices are offset by SetDesc
+    const MatDesc *mats;
+    const OptDesc *opts;
+    const TileDesc *tiles;
+    uint32_t n_tiles;
+    uint32_t pad;
+    unsigned long long *acc; // [out_index * kLimbs + limb]
+    unsigned int *queue;     // [0] tile queue head
+    int *error;              // [0] error flags (bit 0: non-finite payoff, bit 1: fixed-point range)
+    double *dbg_asian;       // optional per-path final values (debug): [(k - dbg_lo) * dbg_mats + j]
+    double *dbg_euro;
+    uint64_t dbg_lo;
+    uint32_t dbg_mats;
+    uint32_t pad2;
+};
+
+} // namespace hexo

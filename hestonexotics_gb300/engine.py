@@ -1,0 +1,290 @@
+"""Python face of the engine: a thin, typed wrapper over the C ABI.
+
+Every computation runs in libhexo_mc.so on the GPU; this module only
+marshals arrays.  ``Engine`` owns one ``hexo_ctx`` (one device, one stream).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+ASIAN = 0
+EUROPEAN = 1
+STEP_REFERENCE = 0
+STEP_GRID = 1
+FP64 = 0
+FP32 = 1
+
+
+@dataclass
+class Params:
+    """HParams (reference src/inc/HDistribution.h:9-24: v_0, v_m, rho, kappa,
+    sigma) plus the rates r and q, which the reference does not have."""
+    v0: float
+    theta: float
+    rho: float
+    kappa: float
+    sigma: float
+    r: float = 0.0
+    q: float = 0.0
+
+    def c(self) -> L.hexo_params:
+        return L.hexo_params(self.v0, self.theta, self.rho, self.kappa, self.sigma, self.r, self.q)
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.v0, self.theta, self.rho, self.kappa, self.sigma, self.r, self.q], dtype=np.float64)
+
+
+@dataclass
+class Config:
+    n_paths: int = 65536
+    step_mode: int = STEP_REFERENCE
+    steps: int = 252
+    steps_per_year: float = 252.0
+    seed: int = 42
+    rng_block_words: int = 16
+    precision: int = FP64
+    block: int = 0
+    paths_per_thread: int = 0
+    unroll: int = 0
+
+    def c(self) -> L.hexo_mc_cfg:
+        return L.hexo_mc_cfg(self.n_paths, self.step_mode, self.steps, self.steps_per_year, self.seed & 0xFFFFFFFF,
+                             self.rng_block_words, self.precision, self.block, self.paths_per_thread, self.unroll)
+
+
+@dataclass
+class Options:
+    """Structure of arrays of options: strike, maturity, payoff kind, paths (0 = config default)."""
+    strike: np.ndarray
+    T: np.ndarray
+    payoff: np.ndarray
+    n_paths: np.ndarray = field(default=None)
+
+    def __post_init__(self):
+        self.strike = np.ascontiguousarray(self.strike, dtype=np.float64)
+        self.T = np.ascontiguousarray(np.broadcast_to(self.T, self.strike.shape), dtype=np.float64)
+        self.payoff = np.ascontiguousarray(np.broadcast_to(self.payoff, self.strike.shape), dtype=np.uint32)
+        if self.n_paths is None:
+            self.n_paths = np.zeros(self.strike.shape, dtype=np.uint64)
+        self.n_paths = np.ascontiguousarray(np.broadcast_to(self.n_paths, self.strike.shape), dtype=np.uint64)
+
+    def __len__(self):
+        return int(self.strike.shape[0])
+
+    def c_array(self):
+        n = len(self)
+        arr = (L.hexo_option * max(n, 1))()
+        for i in range(n):
+            arr[i].strike = float(self.strike[i])
+            arr[i].T = float(self.T[i])
+            arr[i].payoff = int(self.payoff[i])
+            arr[i].reserved = 0
+            arr[i].n_paths = int(self.n_paths[i])
+        return arr
+
+
+@dataclass
+class Request:
+    params: Params
+    S0: float
+    options: Options
+    seed: int = 42
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _u64p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+class Batch:
+    """A batch planned and uploaded once (hexo_batch_prepare), launchable many times."""
+
+    def __init__(self, engine: "Engine", handle: C.c_void_p, keep: list, outputs: list):
+        self.engine = engine
+        self.handle = handle
+        self._keep = keep
+        self.outputs = outputs  # [(price, stderr)] per request
+
+    def launch(self):
+        self.engine._check(L.load().hexo_batch_launch(self.handle))
+
+    def collect(self):
+        self.engine._check(L.load().hexo_batch_collect(self.handle))
+        return self.outputs
+
+    def info(self) -> dict:
+        inf = L.hexo_batch_info()
+        self.engine._check(L.load().hexo_batch_info_get(self.handle, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in L.hexo_batch_info._fields_}
+
+    def close(self):
+        if self.handle:
+            L.load().hexo_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    def __init__(self, device: int = 0, mem_cap_bytes: int = 0, autotune_cache: str | None = None):
+        lib = L.load()
+        self._lib = lib
+        self._ctx = C.c_void_p()
+        opts = L.hexo_ctx_opts(device, mem_cap_bytes, autotune_cache.encode() if autotune_cache else None, 0)
+        st = lib.hexo_ctx_create(C.byref(self._ctx), C.byref(opts))
+        if st != L.HEXO_OK:
+            raise L.HexoError(st, "hexo_ctx_create failed")
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, st: int):
+        if st != L.HEXO_OK:
+            buf = C.create_string_buffer(512)
+            self._lib.hexo_ctx_last_error(self._ctx, buf, 512)
+            raise L.HexoError(st, buf.value.decode(errors="replace"))
+
+    def close(self):
+        if self._ctx:
+            self._lib.hexo_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self._lib.hexo_ctx_stream(self._ctx) or 0
+
+    # ------------------------------------------------------------- pricing
+    def price(self, params: Params, S0: float, options: Options, cfg: Config):
+        n = len(options)
+        price = np.zeros(n)
+        se = np.zeros(n)
+        opts = options.c_array()
+        c = cfg.c()
+        p = params.c()
+        self._check(self._lib.hexo_price(self._ctx, C.byref(p), float(S0), opts, n, C.byref(c), _dp(price), _dp(se)))
+        return price, se
+
+    def _requests(self, requests: Sequence[Request]):
+        arr = (L.hexo_request * len(requests))()
+        keep, outputs = [], []
+        for i, rq in enumerate(requests):
+            n = len(rq.options)
+            opts = rq.options.c_array()
+            price = np.zeros(n)
+            se = np.zeros(n)
+            keep += [opts, price, se]
+            outputs.append((price, se))
+            arr[i].params = rq.params.c()
+            arr[i].S0 = float(rq.S0)
+            arr[i].opts = C.cast(opts, C.POINTER(L.hexo_option))
+            arr[i].n_opts = n
+            arr[i].seed = int(rq.seed) & 0xFFFFFFFF
+            arr[i].price_out = _dp(price)
+            arr[i].stderr_out = _dp(se)
+        keep.append(arr)
+        return arr, keep, outputs
+
+    def price_batch(self, requests: Sequence[Request], cfg: Config):
+        arr, keep, outputs = self._requests(requests)
+        c = cfg.c()
+        self._check(self._lib.hexo_price_batch(self._ctx, arr, len(requests), C.byref(c)))
+        return outputs
+
+    def prepare_batch(self, requests: Sequence[Request], cfg: Config) -> Batch:
+        arr, keep, outputs = self._requests(requests)
+        c = cfg.c()
+        keep.append(c)
+        h = C.c_void_p()
+        self._check(self._lib.hexo_batch_prepare(self._ctx, arr, len(requests), C.byref(c), C.byref(h)))
+        return Batch(self, h, keep, outputs)
+
+    def partial(self, params: Params, S0: float, options: Options, cfg: Config, path_lo: int, path_hi: int):
+        n = len(options)
+        limbs = np.zeros(n * L.HEXO_LIMBS, dtype=np.uint64)
+        opts = options.c_array()
+        c = cfg.c()
+        p = params.c()
+        self._check(self._lib.hexo_price_partial(self._ctx, C.byref(p), float(S0), opts, n, C.byref(c),
+                                                 int(path_lo), int(path_hi), _u64p(limbs)))
+        return limbs.reshape(n, L.HEXO_LIMBS)
+
+    def autotune(self, requests: Sequence[Request], cfg: Config):
+        arr, keep, outputs = self._requests(requests)
+        c = cfg.c()
+        res = L.hexo_tune_result()
+        entries = (L.hexo_tune_entry * 27)()
+        self._check(self._lib.hexo_autotune(self._ctx, arr, len(requests), C.byref(c), C.byref(res), entries, 27))
+        table = [(entries[i].block, entries[i].paths_per_thread, entries[i].unroll, entries[i].ms)
+                 for i in range(res.n_tried)]
+        return {"block": res.block, "paths_per_thread": res.paths_per_thread, "unroll": res.unroll,
+                "best_ms": res.best_ms, "table": table}
+
+    # --------------------------------------------------------------- debug
+    def rng_words(self, seed: int, n_streams: int, n_words: int) -> np.ndarray:
+        out = np.zeros(n_streams * n_words, dtype=np.uint64)
+        self._check(self._lib.hexo_debug_rng_words(self._ctx, seed & 0xFFFFFFFF, n_streams, n_words, _u64p(out)))
+        return out.reshape(n_streams, n_words)
+
+    def rng_draws(self, seed: int, n_streams: int, kinds: np.ndarray) -> np.ndarray:
+        kinds = np.ascontiguousarray(kinds, dtype=np.uint8)
+        out = np.zeros(n_streams * len(kinds))
+        self._check(self._lib.hexo_debug_rng_draws(self._ctx, seed & 0xFFFFFFFF, n_streams,
+                                                   kinds.ctypes.data_as(C.POINTER(C.c_uint8)), len(kinds), _dp(out)))
+        return out.reshape(n_streams, len(kinds))
+
+    def normals(self, words: np.ndarray) -> np.ndarray:
+        words = np.ascontiguousarray(words, dtype=np.uint64)
+        out = np.zeros(len(words))
+        self._check(self._lib.hexo_debug_normals(self._ctx, _u64p(words), len(words), _dp(out)))
+        return out
+
+    def pipe_peaks(self) -> dict:
+        out = np.zeros(4)
+        self._check(self._lib.hexo_debug_pipe_peaks(self._ctx, _dp(out)))
+        return {"fp32_fma": out[0], "fp64_fma": out[1], "mufu": out[2], "int32": out[3]}
+
+    def path_finals(self, params: Params, S0: float, options: Options, cfg: Config, path_lo: int, path_hi: int):
+        n = path_hi - path_lo
+        m_max = len(np.unique(options.T))
+        a = np.zeros(n * m_max)
+        e = np.zeros(n * m_max)
+        nm = C.c_uint32()
+        opts = options.c_array()
+        c = cfg.c()
+        p = params.c()
+        self._check(self._lib.hexo_debug_path_finals(self._ctx, C.byref(p), float(S0), opts, len(options),
+                                                     C.byref(c), path_lo, path_hi, _dp(a), _dp(e), C.byref(nm)))
+        m = nm.value
+        return a[: n * m].reshape(n, m), e[: n * m].reshape(n, m)
+
+
+def finalize_limbs(params: Params, options: Options, cfg: Config, limbs: np.ndarray):
+    """Host-only finalisation of (merged) limb sums; bit-identical to the device finaliser."""
+    lib = L.load()
+    n = len(options)
+    limbs = np.ascontiguousarray(limbs, dtype=np.uint64).reshape(-1)
+    price = np.zeros(n)
+    se = np.zeros(n)
+    p = params.c()
+    c = cfg.c()
+    st = lib.hexo_finalize_limbs(C.byref(p), options.c_array(), n, C.byref(c), _u64p(limbs), _dp(price), _dp(se))
+    if st != L.HEXO_OK:
+        raise L.HexoError(st, "hexo_finalize_limbs")
+    return price, se

@@ -1,0 +1,262 @@
+/*
+ * hexo_mc.h: C ABI of the GB300 Monte Carlo engine for hexo's Heston pricer.
+ *
+ * This is the drop-in boundary for the reference's simulation and pricing
+ * entry point
+ *
+ *   template<class Scheme> std::vector<ffloat> HSimulation::price(
+ *       const HParams& p, const ffloat S, const std::list<options_chain>& all_chains,
+ *       unsigned n_simulations, unsigned n_opts, unsigned steps);
+ *                                         (reference src/inc/HSimulation.h:61-63,
+ *                                          body src/HSimulation.tpp:10-51)
+ *
+ * Everything crosses as plain pointers and sizes.  Buffers are owned by the
+ * caller; no call keeps a pointer after it returns, except the serving
+ * requests, whose option array and output arrays must stay valid until the
+ * request completes.  Errors are status codes, never exceptions; a
+ * message for the last failure of a context is available from
+ * hexo_ctx_last_error().  include/hexo/reference_compat.h wraps this ABI
+ * in the reference's own C++ signature.
+ *
+ * Random numbers.  Path k (0-based) of a request draws from its own stream,
+ * exactly the reference RNG class (src/inc/RNG.h:17-52, src/RNG.cpp:8-47)
+ * constructed as RNG(rng_block_words, (uint32_t)(seed + k)): one SHISHUA
+ * stream seeded {seed + k, 0, 0, 0} filling a uniform buffer first and a
+ * normal buffer next, each refilled from the same stream when it runs dry;
+ * u = (double)word / (double)UINT64_MAX; normals are the float32 AS241
+ * (reference src/as241.f90).  Results therefore do not depend on block
+ * size, paths per thread, batching, sharding or which other requests share
+ * a launch.
+ */
+#ifndef HEXO_MC_H
+#define HEXO_MC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HEXO_ABI_VERSION 1u
+
+typedef enum hexo_status {
+    HEXO_OK = 0,
+    HEXO_ERR_INVALID = 1,      /* bad argument (NaN parameter, T <= 0, zero paths, ...) */
+    HEXO_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    HEXO_ERR_NOMEM = 3,        /* device or host allocation failed */
+    HEXO_ERR_UNSUPPORTED = 4,  /* valid but not supported by this build (e.g. rng_block_words != 16) */
+    HEXO_ERR_TIMEOUT = 5,      /* a bounded wait ran out */
+    HEXO_ERR_NUMERIC = 6,      /* a payoff was not finite or exceeded the fixed-point range */
+    HEXO_ERR_NOT_FOUND = 7,    /* unknown ticket */
+    HEXO_ERR_ADMISSION = 8,    /* request can never fit the device-memory cap */
+    HEXO_ERR_SHUTDOWN = 9      /* server is shutting down */
+} hexo_status;
+
+const char *hexo_status_string(hexo_status s);
+uint32_t hexo_abi_version(void);
+
+/* ---------------------------------------------------------------- context */
+
+typedef struct hexo_ctx hexo_ctx;
+
+typedef struct hexo_ctx_opts {
+    int device;                 /* CUDA device ordinal */
+    uint64_t mem_cap_bytes;     /* device-memory cap for admission; 0 = 32 GiB */
+    const char *autotune_cache; /* file to read/write tuned launch shapes; NULL = none */
+    uint32_t flags;             /* reserved, 0 */
+} hexo_ctx_opts;
+
+hexo_status hexo_ctx_create(hexo_ctx **out, const hexo_ctx_opts *opts /* NULL = defaults */);
+hexo_status hexo_ctx_destroy(hexo_ctx *ctx);
+/* Copies the message of the last failure on this context into buf. */
+hexo_status hexo_ctx_last_error(hexo_ctx *ctx, char *buf, size_t buf_len);
+/* The cudaStream_t (as void*) on which this context launches its kernels. */
+void *hexo_ctx_stream(hexo_ctx *ctx);
+
+/* --------------------------------------------------------------- problem */
+
+/* HParams (reference src/inc/HDistribution.h:9-24, same order) plus the
+ * risk-free rate r and dividend yield q.  r = q = 0 reproduces the
+ * reference, which has neither drift nor discounting. */
+typedef struct hexo_params {
+    double v0, theta, rho, kappa, sigma; /* v_0, v_m, rho, kappa, sigma */
+    double r, q;
+} hexo_params;
+
+typedef enum hexo_payoff {
+    HEXO_ASIAN_CALL = 0,    /* AAsianCallNonAdaptive, src/inc/AsianContract.h:14-48 */
+    HEXO_EUROPEAN_CALL = 1  /* EuropeanCallNonAdaptive, src/inc/VanillaContract.h:14-40 */
+} hexo_payoff;
+
+/* One option: the strike of a reference `option` (src/inc/Types.h:26-33)
+ * plus the time_to_expiry of its `options_chain` (Types.h:37-58). */
+typedef struct hexo_option {
+    double strike;
+    double T;          /* years, > 0 */
+    uint32_t payoff;   /* hexo_payoff */
+    uint32_t reserved; /* 0 */
+    uint64_t n_paths;  /* paths for this option; 0 = hexo_mc_cfg.n_paths */
+} hexo_option;
+
+typedef enum hexo_step_mode {
+    /* the reference's stepping: maturity i is reached with width T_i/steps,
+     * time accumulated as t += width in double (HSimulation.tpp:29,42,84) */
+    HEXO_STEP_REFERENCE = 0,
+    /* the same stepping with steps_i = max(5, round(steps_per_year * T_i)) */
+    HEXO_STEP_GRID = 1
+} hexo_step_mode;
+
+typedef enum hexo_precision {
+    HEXO_FP64 = 0, /* plain form: paths in FP64 */
+    HEXO_FP32 = 1  /* paths in FP32; AS241 float32 as in the reference; FP64 finalisation */
+} hexo_precision;
+
+typedef struct hexo_mc_cfg {
+    uint64_t n_paths;         /* default paths per option (n_simulations) */
+    uint32_t step_mode;       /* hexo_step_mode */
+    uint32_t steps;           /* REFERENCE mode: steps per maturity */
+    double steps_per_year;    /* GRID mode; 0 = 252 */
+    uint32_t seed;            /* default seed for hexo_price */
+    uint32_t rng_block_words; /* RNG buffer size in 64-bit words; 0 = 16; the GPU supports 16 */
+    uint32_t precision;       /* hexo_precision */
+    uint32_t block;           /* launch shape override: threads per CTA, 0 = tuned/default */
+    uint32_t paths_per_thread;/* 0 = tuned/default */
+    uint32_t unroll;          /* 0 = tuned/default */
+} hexo_mc_cfg;
+
+/* Fills cfg with the defaults: 65,536 paths, REFERENCE stepping with 252
+ * steps, seed 42, 16-word RNG buffers, FP64, tuned launch shape. */
+void hexo_mc_cfg_default(hexo_mc_cfg *cfg);
+
+/* ------------------------------------------------------- plain pricing */
+
+/* Prices n_opts options on one parameter set; blocks until done.
+ * price_out[i]  = exp(-r T_i) * mean payoff of option i
+ * stderr_out[i] = standard error of price_out[i] (may be NULL). */
+hexo_status hexo_price(hexo_ctx *ctx, const hexo_params *p, double S0, const hexo_option *opts,
+                       uint32_t n_opts, const hexo_mc_cfg *cfg, double *price_out, double *stderr_out);
+
+/* ------------------------------------------------------ batched pricing */
+
+typedef struct hexo_request {
+    hexo_params params;
+    double S0;
+    const hexo_option *opts;
+    uint32_t n_opts;
+    uint32_t seed;
+    double *price_out;   /* n_opts */
+    double *stderr_out;  /* n_opts, may be NULL */
+} hexo_request;
+
+/* Prices many parameter sets in one persistent launch. */
+hexo_status hexo_price_batch(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg);
+
+/* A batch planned and uploaded once, launchable many times (a captured CUDA
+ * graph); used for repeated pricing of the same shapes and for timing. */
+typedef struct hexo_batch hexo_batch;
+
+typedef struct hexo_batch_info {
+    uint64_t nominal_path_steps;  /* sum over paths of the grid steps to the path's last maturity */
+    uint64_t executed_path_steps; /* QE steps actually executed (includes the reference's extra steps) */
+    uint64_t n_paths;             /* simulated paths */
+    uint32_t n_tiles, n_sets, n_options, block, paths_per_thread, unroll, grid;
+    uint64_t device_bytes;        /* device memory the batch holds */
+    uint64_t h2d_bytes;           /* bytes uploaded when the batch is planned (descriptors) */
+    uint64_t d2h_bytes;           /* bytes copied back per run (prices, standard errors, status) */
+    double last_kernel_ms;        /* path-kernel time of the last collected run (CUDA events) */
+} hexo_batch_info;
+
+hexo_status hexo_batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                               hexo_batch **out);
+/* Enqueues one run on the context stream (graph launch); returns at once. */
+hexo_status hexo_batch_launch(hexo_batch *b);
+/* Waits for the last launch and copies prices / standard errors into the
+ * requests' output arrays. */
+hexo_status hexo_batch_collect(hexo_batch *b);
+hexo_status hexo_batch_info_get(hexo_batch *b, hexo_batch_info *info);
+hexo_status hexo_batch_destroy(hexo_batch *b);
+
+/* --------------------------------------------------------------- shards */
+
+/* Exact partial sums over paths [path_lo, path_hi) of one request: for each
+ * option six uint64 limbs (sum round(pay*2^40) and sum round(pay^2*2^24),
+ * each split into three 25-bit limb sums).  Limb sums of disjoint path
+ * ranges add exactly, so any split across shards or devices merges to the
+ * bit-identical result of one launch. */
+#define HEXO_LIMBS 6
+hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, const hexo_option *opts,
+                               uint32_t n_opts, const hexo_mc_cfg *cfg, uint64_t path_lo, uint64_t path_hi,
+                               uint64_t *limbs_out /* n_opts * HEXO_LIMBS */);
+/* Host-only: prices and standard errors from (merged) limb sums; the same
+ * operation sequence as the device finaliser, so results match it bit for bit. */
+hexo_status hexo_finalize_limbs(const hexo_params *p, const hexo_option *opts, uint32_t n_opts,
+                                const hexo_mc_cfg *cfg, const uint64_t *limbs, double *price_out,
+                                double *stderr_out);
+
+/* ------------------------------------------------------------- planning */
+
+/* Host-only (no GPU needed): the work a batch represents. */
+typedef struct hexo_plan_stats {
+    uint64_t nominal_path_steps;  /* grid steps to each path's last maturity, summed over paths */
+    uint64_t executed_path_steps; /* QE steps the kernel executes for active paths */
+    uint64_t n_paths;             /* simulated paths */
+    uint32_t n_maturities, n_segments, n_tiles, n_options;
+} hexo_plan_stats;
+hexo_status hexo_plan_stats_get(const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                                hexo_plan_stats *out);
+
+/* Host-only: the step schedule of one request.  For each distinct maturity j
+ * (ascending): steps executed up to and including the step that prices it,
+ * and T_j - t_prev of that step.  Returns the number of maturities in
+ * *n_mats; arrays must hold `cap` entries. */
+hexo_status hexo_plan_schedule(const hexo_params *p, double S0, const hexo_option *opts, uint32_t n_opts,
+                               const hexo_mc_cfg *cfg, uint32_t cap, uint64_t *steps_to_mat, double *tmtp,
+                               double *maturity, uint32_t *n_mats);
+
+/* ------------------------------------------------------------- autotune */
+
+typedef struct hexo_tune_result {
+    uint32_t block, paths_per_thread, unroll, n_tried;
+    double best_ms;
+} hexo_tune_result;
+
+typedef struct hexo_tune_entry {
+    uint32_t block, paths_per_thread, unroll;
+    float ms;
+} hexo_tune_entry;
+
+/* Sweeps threads per CTA {128,256,512} x paths per thread {1,2,4} x step
+ * unroll {1,2,4} (shapes that do not fit an SM are skipped) on the given
+ * requests, times one launch of each, and makes the fastest the context's
+ * shape for cfg->precision (saved to the context's autotune cache file when
+ * one was given).  entries (may be NULL) receives up to max_entries timings. */
+hexo_status hexo_autotune(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                          hexo_tune_result *result, hexo_tune_entry *entries, uint32_t max_entries);
+
+/* ---------------------------------------------------------------- debug */
+
+/* Raw SHISHUA words of streams seed+k, k in [0, n_streams): out[k*n_words + i]. */
+hexo_status hexo_debug_rng_words(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, uint32_t n_words,
+                                 uint64_t *out);
+/* Draws of RNG(16, seed + k) for n_streams streams following one shared
+ * kinds[] sequence (0 = normal, 1 = uniform); out[k*n + i]. */
+hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, const uint8_t *kinds,
+                                 uint32_t n, double *out);
+/* AS241 of u = (double)w / (double)UINT64_MAX for each word: out[i]. */
+hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n, double *out);
+/* Measured lane-operation rates (per second) of this GPU's pipes, from
+ * throughput probes: out4 = {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD}. */
+hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out4);
+/* Per-path final values (Asian average, interpolated terminal spot) at every
+ * distinct maturity for paths [path_lo, path_hi); NaN after a path's last
+ * maturity.  Arrays are [(k - path_lo) * n_mats + j]; n_mats_out receives
+ * the number of distinct maturities. */
+hexo_status hexo_debug_path_finals(hexo_ctx *ctx, const hexo_params *p, double S0, const hexo_option *opts,
+                                   uint32_t n_opts, const hexo_mc_cfg *cfg, uint64_t path_lo, uint64_t path_hi,
+                                   double *asian_out, double *euro_out, uint32_t *n_mats_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

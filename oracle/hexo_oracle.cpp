@@ -1,0 +1,405 @@
+/*
+ * ORACLE / TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement ("port") of the reference's Monte Carlo pricing path, used
+ * as the parity checker for the GPU engine and as the timed CPU baseline.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * it; the product never links or calls it.
+ *
+ * What it restates (reference file:line):
+ *   OracleRNG        RNG wrapper, src/inc/RNG.h:17-52 + src/RNG.cpp:8-47:
+ *                    one SHISHUA stream seeded {seed,0,0,0} feeds a uniform
+ *                    buffer (filled first) and a normal buffer (filled next);
+ *                    each refills from the same stream when it runs dry;
+ *                    u = (double)w / (double)UINT64_MAX (RNG.cpp:31); normals
+ *                    are ppnd16(u) (RNG.cpp:34-43).
+ *   qe_step          HQEAnderson::operator++, src/HSimulation.tpp:52-86, with
+ *                    an optional (r-q)*delta drift folded into K_0 (zero drift
+ *                    leaves every operation bit-identical).
+ *   run_path         the per-path body of HSimulation::price,
+ *                    src/HSimulation.tpp:30-46, with the Asian contract
+ *                    (src/inc/AsianContract.h:25-47) and the European contract
+ *                    (src/inc/VanillaContract.h:28-39) tracked on one path.
+ *   reference partition driver: price()'s thread partition
+ *                    (HSimulation.tpp:23-29: n/threads paths per thread, one
+ *                    RNG(RAND_BUF_SIZE=2^20, 1<<tid) per thread, the trailing
+ *                    step after the last maturity) with the per-option
+ *                    accumulation `prices[i] += payoff/n` (tpp:40) kept in
+ *                    path order but race-free (per-thread arrays).
+ *   per-path driver: the stream partition the GPU engine uses: path k of a
+ *                    request draws from its own RNG(block_words, seed+k).
+ *
+ * Built twice by oracle/Makefile: liboracle.so (-O2 -ffp-contract=off, the
+ * parity checker) and liboracle_fast.so (the reference's release flags minus
+ * -march=native, the timed CPU baseline).  as241.c is always compiled
+ * without fast-math, as the reference compiles as241.f90.
+ */
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#include <numeric>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "shishua.h"
+
+extern "C" double ppnd16(double *, int *);
+extern "C" float oracle_logf(float);
+
+namespace {
+
+/* RNG.h:17-52, RNG.cpp:8-47 */
+class OracleRNG {
+    std::vector<double> u_, g_;
+    size_t cu_, cg_, size_;
+    prng_state s_;
+    void fill_uniform(std::vector<double> &buf) {
+        prng_gen(&s_, reinterpret_cast<uint8_t *>(buf.data()), size_ * sizeof(double));
+        for (double &x : buf) {
+            uint64_t w;
+            std::memcpy(&w, &x, 8);
+            x = static_cast<double>(w) / static_cast<double>(UINT64_MAX);
+        }
+    }
+    void fill_normal() {
+        fill_uniform(g_);
+        for (double &x : g_) {
+            int ifault = 0;
+            x = ppnd16(&x, &ifault);
+        }
+    }
+
+public:
+    OracleRNG(size_t size, uint64_t seed0) : u_(size), g_(size), cu_(0), cg_(0), size_(size) {
+        uint64_t seed[4] = {seed0, 0, 0, 0};
+        prng_init(&s_, seed);
+        fill_uniform(u_);
+        fill_normal();
+    }
+    double grand() {
+        if (cg_ == size_) { fill_normal(); cg_ = 0; }
+        return g_[cg_++];
+    }
+    double urand() {
+        if (cu_ == size_) { fill_uniform(u_); cu_ = 0; }
+        return u_[cu_++];
+    }
+};
+
+struct Params { double v0, theta, rho, kappa, sigma, r, q; };
+
+struct PathState { double Xc, Xp, vc, vp, t, tp, logX; };
+
+/* HSimulation.tpp:52-86 (+ drift in K_0) */
+inline void qe_step(PathState &st, const Params &p, double delta, OracleRNG &rng) {
+    const double v_0 = p.v0, theta = p.theta, rho = p.rho, kappa = p.kappa, eps = p.sigma;
+    (void)v_0;
+    const double gamma_1 = .5, gamma_2 = .5;
+    double discount = std::exp(-kappa * delta);
+    double m = theta + (st.vc - theta) * discount;
+    double sp2 = std::fabs(st.vc * eps * eps * discount / kappa * (1 - discount) +
+                           theta * eps * eps / (2 * kappa) * (1. - discount) * (1. - discount));
+    double Psi = sp2 / (m * m);
+    st.vp = st.vc;
+    if (Psi < 1.5) {
+        double bp2 = 2 / Psi - 1 + std::sqrt(2 / Psi * (2 / Psi - 1));
+        double b = std::sqrt(bp2);
+        double a = m / (1 + bp2);
+        double Z_V = rng.grand();
+        st.vc = a * (b + Z_V) * (b + Z_V);
+    } else {
+        double pp = (Psi - 1) / (Psi + 1);
+        double beta = 2 / (m * (Psi + 1));
+        double U_V = rng.urand();
+        st.vc = pp < U_V ? std::log((1 - pp) / (1 - U_V)) / beta : 0.;
+    }
+    double K_0 = -rho * kappa * theta / eps * delta + (p.r - p.q) * delta;
+    double K_1 = gamma_1 * delta * (kappa * rho / eps - .5) - rho / eps;
+    double K_2 = gamma_2 * delta * (kappa * rho / eps - .5) + rho / eps;
+    double K_3 = gamma_1 * delta * (1 - rho * rho);
+    double K_4 = gamma_2 * delta * (1 - rho * rho);
+    st.logX = st.logX + K_0 + K_1 * st.vp + K_2 * st.vc + std::sqrt(K_3 * st.vp + K_4 * st.vc) * rng.grand();
+    st.Xp = st.Xc;
+    st.Xc = std::exp(st.logX);
+    st.tp = st.t;
+    st.t += delta;
+}
+
+/* Maturity-grouped view of one pricing request. */
+struct Problem {
+    Params p;
+    double S0;
+    std::vector<double> T;           // distinct maturities, ascending
+    std::vector<uint32_t> steps;     // steps per maturity (the reference's `steps` argument)
+    std::vector<std::vector<uint32_t>> opts; // option indices per maturity
+    const double *strike;
+    const uint8_t *kind;             // 0 = arithmetic Asian call, 1 = European call
+    const uint64_t *n_paths;         // per option
+    uint32_t n_opts;
+};
+
+/* Per-path body of HSimulation.tpp:30-46.  `visit(j, asian_final, euro_final)`
+ * is called at each maturity j in increasing order; it returns false once the
+ * path is no longer needed.  `trailing` runs the extra step the reference's
+ * for-increment takes after the last pricing (tpp:35), which matters only
+ * when the stream is shared with the next path. */
+template <class Visit>
+inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&visit) {
+    PathState st{pr.S0, pr.S0, pr.p.v0, pr.p.v0, 0., 0., std::log(pr.S0)};
+    const size_t m = pr.T.size();
+    size_t j = 0;
+    double dt = pr.T[0] / pr.steps[0];  // update_earliest, AsianContract.h:35-38
+    double acc = 0.;                    // reset, AsianContract.h:39-42
+    qe_step(st, pr.p, dt, rng);         // ++(heston_sde = initial_state), tpp:35
+    for (;;) {
+        bool more = true;
+        while (j < m && st.t >= pr.T[j]) {                              // tpp:36
+            double T = pr.T[j];
+            double interp = (st.Xc - st.Xp) * (T - st.tp) / dt;
+            double asian = (acc + interp) / T;                          // AsianContract.h:29-34
+            double euro = st.Xp + (st.Xc - st.Xp) * (T - st.tp) / dt;   // VanillaContract.h:28-31
+            more = visit(j, asian, euro);
+            ++j;
+            if (j < m) dt = pr.T[j] / pr.steps[j];                      // tpp:41-42
+            if (!more) break;
+        }
+        if (j >= m || !more) {
+            if (trailing) qe_step(st, pr.p, dt, rng);                   // tpp:35 for-increment
+            return;
+        }
+        acc += dt * .5 * (st.Xc + st.Xp);                               // AsianContract.h:25-28
+        qe_step(st, pr.p, dt, rng);
+    }
+}
+
+inline double payoff_of(const Problem &pr, uint32_t o, double asian, double euro) {
+    double fv = pr.kind[o] == 0 ? asian : euro;
+    return std::max(0., fv - pr.strike[o]);                             // AsianContract.h:43-47
+}
+
+/* Exact fixed-point accumulation in the engine's format: q = round(pay*2^40)
+ * and q2 = round(pay^2*2^24) (ties to even), each split into three 25-bit
+ * limbs; limb sums are exact, so the order of paths does not matter. */
+struct ExactSums {
+    std::vector<uint64_t> l;   // [o*6 + limb]
+    explicit ExactSums(size_t n) : l(6 * n, 0) {}
+    void add(uint32_t o, double pay) {
+        const unsigned __int128 q = (unsigned __int128)std::nearbyint(pay * 0x1p40);
+        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(pay * pay * 0x1p24);
+        const uint64_t M = (1ull << 25) - 1;
+        uint64_t *d = &l[6 * (size_t)o];
+        d[0] += (uint64_t)(q & M); d[1] += (uint64_t)((q >> 25) & M); d[2] += (uint64_t)(q >> 50);
+        d[3] += (uint64_t)(q2 & M); d[4] += (uint64_t)((q2 >> 25) & M); d[5] += (uint64_t)(q2 >> 50);
+    }
+    void merge(const ExactSums &o) {
+        for (size_t i = 0; i < l.size(); ++i) l[i] += o.l[i];
+    }
+    static unsigned __int128 value(const uint64_t *d) {
+        return (unsigned __int128)d[0] + ((unsigned __int128)d[1] << 25) + ((unsigned __int128)d[2] << 50);
+    }
+};
+
+int build_problem(Problem &pr, const double *params7, double S0, uint32_t n_opts, const double *strike,
+                  const double *T, const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode,
+                  uint32_t steps, double steps_per_year) {
+    if (n_opts == 0) return 1;
+    pr.p = Params{params7[0], params7[1], params7[2], params7[3], params7[4], params7[5], params7[6]};
+    pr.S0 = S0;
+    pr.strike = strike;
+    pr.kind = kind;
+    pr.n_paths = n_paths;
+    pr.n_opts = n_opts;
+    std::vector<uint32_t> idx(n_opts);
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return T[a] < T[b]; });
+    for (uint32_t i : idx) {
+        if (!(T[i] > 0.)) return 2;
+        if (pr.T.empty() || pr.T.back() != T[i]) {
+            pr.T.push_back(T[i]);
+            uint32_t n = steps;
+            if (step_mode == 1) {
+                double g = std::nearbyint(steps_per_year * T[i]);
+                n = static_cast<uint32_t>(std::max(5.0, g));
+            }
+            if (n == 0) return 3;
+            pr.steps.push_back(n);
+            pr.opts.emplace_back();
+        }
+        pr.opts.back().push_back(i);
+    }
+    return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+/* Raw SHISHUA words of the stream seeded {seed4}. */
+void oracle_shishua_words(const uint64_t seed4[4], uint64_t n_words, uint64_t *out) {
+    prng_state s;
+    uint64_t seed[4] = {seed4[0], seed4[1], seed4[2], seed4[3]};
+    prng_init(&s, seed);
+    std::vector<uint8_t> blk(128);
+    for (uint64_t w = 0; w < n_words; w += 16) {
+        prng_gen(&s, blk.data(), 128);
+        for (uint64_t k = 0; k < 16 && w + k < n_words; ++k) std::memcpy(&out[w + k], &blk[8 * k], 8);
+    }
+}
+
+/* Draws of RNG(block_words, seed): kinds[i] = 0 -> get_grand, 1 -> get_urand. */
+void oracle_rng_draws(uint32_t seed, uint32_t block_words, const uint8_t *kinds, uint64_t n, double *out) {
+    OracleRNG rng(block_words, seed);
+    for (uint64_t i = 0; i < n; ++i) out[i] = kinds[i] ? rng.urand() : rng.grand();
+}
+
+double oracle_ppnd16(double p, int *ifault) { return ppnd16(&p, ifault); }
+
+/* ppnd16 of u = (double)w / (double)UINT64_MAX for each word (RNG.cpp:31-41). */
+void oracle_normals(const uint64_t *words, uint64_t n, double *out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        double u = static_cast<double>(words[i]) / static_cast<double>(UINT64_MAX);
+        int ifault = 0;
+        out[i] = ppnd16(&u, &ifault);
+    }
+}
+float oracle_logf_c(float x) { return oracle_logf(x); }
+
+/*
+ * Per-path stream partition (the GPU engine's): path k uses
+ * RNG(block_words, (uint32)(seed + k)); option o is priced on paths
+ * k < n_paths[o].  Outputs per option, over paths [path_lo, path_hi):
+ * discounted price, its standard error, and six limb sums (the engine's
+ * format: 25-bit limbs of round(pay*2^40) and round(pay^2*2^24)).
+ * params7 = {v0, theta(v_m), rho, kappa, sigma, r, q}; HParams order,
+ * src/inc/HDistribution.h:9-24.  step_mode 0 = the reference's T_i/steps
+ * stepping; 1 = max(5, round(steps_per_year*T_i)) steps per maturity.
+ */
+int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
+                       const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
+                       double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                       uint64_t path_hi, int n_threads, double *price, double *stderr_out, uint64_t *limbs_out) {
+    Problem pr;
+    int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
+    if (rc) return rc;
+    if (block_words == 0 || (block_words * 8) % 128 != 0) return 4;  // RNG.cpp:10
+    // last maturity index each path needs
+    std::vector<uint64_t> mat_paths(pr.T.size(), 0);
+    for (size_t j = 0; j < pr.T.size(); ++j)
+        for (uint32_t o : pr.opts[j]) mat_paths[j] = std::max(mat_paths[j], n_paths[o]);
+    uint64_t n_max = *std::max_element(mat_paths.begin(), mat_paths.end());
+    path_hi = std::min(path_hi, n_max);
+    int nt = n_threads > 0 ? n_threads : 1;
+    std::vector<ExactSums> part(nt, ExactSums(n_opts));
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+    for (int64_t k = (int64_t)path_lo; k < (int64_t)path_hi; ++k) {
+#ifdef _OPENMP
+        ExactSums &acc = part[omp_get_thread_num()];
+#else
+        ExactSums &acc = part[0];
+#endif
+        size_t last = 0;
+        for (size_t j = 0; j < pr.T.size(); ++j)
+            if (mat_paths[j] > (uint64_t)k) last = j;
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        run_path(pr, rng, false, [&](size_t j, double asian, double euro) {
+            for (uint32_t o : pr.opts[j])
+                if ((uint64_t)k < n_paths[o]) acc.add(o, payoff_of(pr, o, asian, euro));
+            return j < last;
+        });
+    }
+    for (int t = 1; t < nt; ++t) part[0].merge(part[t]);
+    for (uint32_t o = 0; o < n_opts; ++o) {
+        const uint64_t *d = &part[0].l[6 * (size_t)o];
+        if (limbs_out) std::memcpy(&limbs_out[6 * (size_t)o], d, 6 * sizeof(uint64_t));
+        const unsigned __int128 s1 = ExactSums::value(d), s2 = ExactSums::value(d + 3);
+        const uint64_t hi = std::min<uint64_t>(n_paths[o], path_hi);
+        const double n = hi > path_lo ? (double)(hi - path_lo) : 0.0;
+        const long double mean = n > 0 ? ((long double)s1 / 0x1p40L) / n : 0.L;
+        const long double m2 = n > 0 ? ((long double)s2 / 0x1p24L) / n : 0.L;
+        long double var = n > 1 ? (m2 - mean * mean) * n / (n - 1) : 0.L;
+        if (var < 0) var = 0;
+        const double disc = std::exp(-pr.p.r * T[o]);
+        if (price) price[o] = disc * (double)mean;
+        if (stderr_out) stderr_out[o] = n > 0 ? disc * std::sqrt((double)(var / n)) : 0.0;
+    }
+    return 0;
+}
+
+/*
+ * Final values per path (debug / localisation): for each path k in
+ * [path_lo, path_hi) and each distinct maturity j, the Asian average and
+ * the interpolated terminal spot, NaN where the path stops earlier.
+ * out arrays are [(k - path_lo) * n_mats + j]; n_mats_out receives the count.
+ */
+int oracle_path_finals(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
+                       const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
+                       double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                       uint64_t path_hi, double *asian_out, double *euro_out, uint32_t *n_mats_out) {
+    Problem pr;
+    int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
+    if (rc) return rc;
+    const size_t m = pr.T.size();
+    if (n_mats_out) *n_mats_out = (uint32_t)m;
+    std::vector<uint64_t> mat_paths(m, 0);
+    for (size_t j = 0; j < m; ++j)
+        for (uint32_t o : pr.opts[j]) mat_paths[j] = std::max(mat_paths[j], n_paths[o]);
+    for (uint64_t k = path_lo; k < path_hi; ++k) {
+        size_t last = 0;
+        bool any = false;
+        for (size_t j = 0; j < m; ++j)
+            if (mat_paths[j] > k) { last = j; any = true; }
+        for (size_t j = 0; j < m; ++j) {
+            asian_out[(k - path_lo) * m + j] = NAN;
+            euro_out[(k - path_lo) * m + j] = NAN;
+        }
+        if (!any) continue;
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + k));
+        run_path(pr, rng, false, [&](size_t j, double asian, double euro) {
+            asian_out[(k - path_lo) * m + j] = asian;
+            euro_out[(k - path_lo) * m + j] = euro;
+            return j < last;
+        });
+    }
+    return 0;
+}
+
+/*
+ * The reference's own partition (HSimulation.tpp:23-49): n_threads "threads",
+ * each with RNG(buf_words, 1<<tid) and n/n_threads consecutive paths sharing
+ * that stream, the trailing step included, every path pricing every option,
+ * prices[o] = sum over paths of payoff/n in path order (undiscounted, as the
+ * reference returns).  With n_threads == 1 and buf_words == 2^20 this equals
+ * the untouched HSimulation::price<> on one OpenMP thread.  `omp_threads`
+ * runs the partition's threads concurrently (each into its own array,
+ * merged in thread order).  Returns the number of paths simulated.
+ */
+int64_t oracle_price_reference_partition(const double *params7, double S0, uint32_t n_opts, const double *strike,
+                                         const double *T, const uint8_t *kind, uint32_t steps, uint32_t n_sims,
+                                         int n_threads, uint32_t buf_words, int omp_threads, double *prices) {
+    std::vector<uint64_t> all(n_opts, n_sims);
+    Problem pr;
+    if (build_problem(pr, params7, S0, n_opts, strike, T, kind, all.data(), 0, steps, 252.)) return -1;
+    const int nt = n_threads > 0 ? n_threads : 1;
+    const uint32_t local_sims = n_sims / (uint32_t)nt;                  // tpp:27
+    std::vector<std::vector<double>> local(nt, std::vector<double>(n_opts, 0.));
+#pragma omp parallel for num_threads(omp_threads > 0 ? omp_threads : 1) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        OracleRNG rng(buf_words, 1u << t);                              // tpp:28
+        std::vector<double> &pr_t = local[t];
+        for (uint32_t i = 0; i < local_sims; ++i)
+            run_path(pr, rng, true, [&](size_t j, double asian, double euro) {
+                for (uint32_t o : pr.opts[j]) pr_t[o] += payoff_of(pr, o, asian, euro) / n_sims;  // tpp:40
+                return true;
+            });
+    }
+    for (uint32_t o = 0; o < n_opts; ++o) {
+        double s = 0.;
+        for (int t = 0; t < nt; ++t) s += local[t][o];
+        prices[o] = s;
+    }
+    return (int64_t)local_sims * nt;
+}
+
+} // extern "C"

@@ -1,0 +1,221 @@
+"""GPU pricing against the oracle and the reference golden vectors.
+
+Tolerances (written where used):
+  * FP64 form vs the oracle / reference payoffs: 1e-10 relative on prices
+    (absolute 1e-12 * S0 for prices that are essentially zero), the bar the
+    plain form is held to; per-path final values to 1e-12 relative.
+  * FP32 form vs the FP64 oracle on the same streams: 1e-4 relative for
+    prices above 1e-3 * S0, and inside one standard error everywhere.
+  * Launch shapes, batching, graphs and shards: bit-identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, unhex
+from hestonexotics_gb300 import engine as E
+from hestonexotics_gb300 import workloads as W
+from hestonexotics_gb300._lib import HexoError
+
+pytestmark = pytest.mark.gpu
+
+FP64_REL = 1e-10
+
+
+def oracle_price(oracle, req, cfg, **kw):
+    o = req.options
+    return oracle.price_paths(req.params.as_array(), req.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths,
+                              n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
+                              steps_per_year=cfg.steps_per_year, seed=req.seed, **kw)
+
+
+def assert_fp64_close(got, want, S0):
+    np.testing.assert_allclose(got, want, rtol=FP64_REL, atol=1e-12 * S0)
+
+
+def test_plain_asian_fp64(engine, oracle):
+    req, cfg = W.plain_asian()
+    p, se = engine.price(req.params, req.S0, req.options, cfg)
+    op, ose, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p, op, req.S0)
+    np.testing.assert_allclose(se, ose, rtol=1e-8)
+    assert 2.0 < p[0] < 8.0 and 0 < se[0] < 0.1
+
+
+def test_golden_reference_payoffs(engine):
+    # per-path payoffs from the reference's own classes, one RNG(16, 42 + k) per path
+    for case in golden("ref_paths.json"):
+        T = np.repeat(case["T"], [len(s) for s in case["strikes"]])
+        K = np.array([k for s in case["strikes"] for k in s])
+        n = case["n_paths"]
+        opts = E.Options(K, T, case["kind"])
+        cfg = E.Config(n_paths=n, steps=case["steps"], seed=case["seed"])
+        params = E.Params(*case["params5"])
+        p, se = engine.price(params, case["S"], opts, cfg)
+        pay = unhex(case["payoffs"]).reshape(n, len(K))
+        np.testing.assert_allclose(p, pay.mean(axis=0), rtol=FP64_REL, atol=1e-12 * case["S"])
+        asian, euro = engine.path_finals(params, case["S"], opts, cfg, 0, n)
+        finals = asian if case["kind"] == 0 else euro
+        mat = np.searchsorted(np.unique(T), T)
+        np.testing.assert_allclose(np.maximum(0.0, finals[:, mat] - K), pay, rtol=1e-12, atol=1e-12 * case["S"])
+
+
+def test_path_finals_fp64(engine, oracle):
+    req, cfg = W.single_chain(n_paths=700)
+    cfg.steps = 40
+    cfg.step_mode = E.STEP_REFERENCE
+    o = req.options
+    ga, ge = engine.path_finals(req.params, req.S0, o, cfg, 0, 700)
+    oa, oe = oracle.path_finals(req.params.as_array(), req.S0, o.strike, o.T, o.payoff.astype(np.uint8),
+                                n_default=700, steps=40, seed=req.seed, path_lo=0, path_hi=700)
+    np.testing.assert_allclose(ga, oa, rtol=1e-12)
+    np.testing.assert_allclose(ge, oe, rtol=1e-12)
+
+
+@pytest.mark.parametrize("mode", [E.STEP_REFERENCE, E.STEP_GRID])
+def test_chain_fp64(engine, oracle, mode):
+    req, cfg = W.single_chain(n_paths=1 << 13)
+    cfg.step_mode = mode
+    cfg.steps = 50
+    p, se = engine.price(req.params, req.S0, req.options, cfg)
+    op, ose, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p, op, req.S0)
+    np.testing.assert_allclose(se, ose, rtol=1e-7, atol=1e-12)
+
+
+def test_feller_violating_fp64(engine, oracle):
+    req, cfg = W.feller_violating(n_paths=1 << 12)
+    p, se = engine.price(req.params, req.S0, req.options, cfg)
+    op, _, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p, op, req.S0)
+
+
+def fp32_check(p32, se32, p64, S0):
+    big = p64 > 1e-3 * S0
+    rel = np.abs(p32 - p64) / np.where(big, p64, 1.0)
+    assert rel[big].max() <= 1e-4, rel[big].max()
+    assert np.all(np.abs(p32 - p64) <= np.maximum(se32, 1e-9 * S0))
+
+
+@pytest.mark.parametrize("maker", [W.single_chain, W.feller_violating])
+def test_fp32_vs_fp64_oracle(engine, oracle, maker):
+    req, cfg = maker(n_paths=1 << 14)
+    p64, _, _ = oracle_price(oracle, req, cfg)
+    cfg.precision = E.FP32
+    p32, se32 = engine.price(req.params, req.S0, req.options, cfg)
+    fp32_check(p32, se32, p64, req.S0)
+
+
+def test_launch_shapes_bit_identical(engine):
+    req, cfg = W.single_chain(n_paths=5000)
+    cfg.steps_per_year = 52.0
+    ref = None
+    for prec in (E.FP64, E.FP32):
+        cfg.precision = prec
+        ref = None
+        for block, ppt, unroll in [(256, 1, 1), (128, 1, 2), (512, 1, 4), (128, 2, 1), (256, 2, 2), (128, 4, 1)]:
+            cfg.block, cfg.paths_per_thread, cfg.unroll = block, ppt, unroll
+            p, se = engine.price(req.params, req.S0, req.options, cfg)
+            if ref is None:
+                ref = (p, se)
+            assert np.array_equal(p, ref[0]) and np.array_equal(se, ref[1]), (prec, block, ppt, unroll)
+
+
+def test_batch_equals_alone(engine):
+    reqs, cfg = W.uneven_batch(n_sets=5, path_scale=1 / 256, precision=E.FP32)
+    mixed = engine.price_batch(reqs, cfg)
+    for rq, (p, se) in zip(reqs, mixed):
+        alone = engine.price_batch([rq], cfg)[0]
+        assert np.array_equal(p, alone[0]) and np.array_equal(se, alone[1])
+
+
+def test_prepared_graph_relaunch(engine):
+    reqs, cfg = W.uneven_batch(n_sets=3, path_scale=1 / 512, precision=E.FP32)
+    b = engine.prepare_batch(reqs, cfg)
+    b.launch()
+    first = [(p.copy(), s.copy()) for p, s in b.collect()]
+    b.launch()
+    b.launch()
+    second = b.collect()
+    for (p1, s1), (p2, s2) in zip(first, second):
+        assert np.array_equal(p1, p2) and np.array_equal(s1, s2)
+    direct = engine.price_batch(reqs, cfg)
+    for (p1, _), (p2, _) in zip(first, direct):
+        assert np.array_equal(p1, p2)
+    info = b.info()
+    assert info["nominal_path_steps"] > 0 and info["n_sets"] == 3
+    b.close()
+
+
+def test_uneven_batch_fp64_vs_oracle(engine, oracle):
+    reqs, cfg = W.uneven_batch(n_sets=3, path_scale=1 / 256, precision=E.FP64)
+    out = engine.price_batch(reqs, cfg)
+    for rq, (p, _) in zip(reqs, out):
+        op, _, _ = oracle_price(oracle, rq, cfg)
+        assert_fp64_close(p, op, rq.S0)
+
+
+def test_shards_merge_bit_identical(engine):
+    req, cfg = W.single_chain(n_paths=6000)
+    cfg.steps_per_year = 100.0
+    full = engine.partial(req.params, req.S0, req.options, cfg, 0, 6000)
+    a = engine.partial(req.params, req.S0, req.options, cfg, 0, 2500)
+    b = engine.partial(req.params, req.S0, req.options, cfg, 2500, 6000)
+    assert np.array_equal(full, a + b)
+    p_merge, se_merge = E.finalize_limbs(req.params, req.options, cfg, a + b)
+    p, se = engine.price(req.params, req.S0, req.options, cfg)
+    assert np.array_equal(p, p_merge) and np.array_equal(se, se_merge)
+
+
+def test_limbs_match_oracle_exactly_where_payoffs_do(engine, oracle):
+    # FP64 payoffs agree with the oracle to ~1e-16; their fixed-point sums then agree to a few units
+    req, cfg = W.plain_asian(n_paths=3000)
+    g = engine.partial(req.params, req.S0, req.options, cfg, 0, 3000)
+    _, _, o = oracle_price(oracle, req, cfg)
+    v = lambda l: int(l[0]) + (int(l[1]) << 25) + (int(l[2]) << 50)
+    assert abs(v(g[0]) - v(o[0])) <= 3000
+
+
+def test_ragged_paths_and_many_options(engine, oracle):
+    rng = np.random.default_rng(5)
+    n = 150
+    T = np.repeat([0.1, 0.35, 0.35001, 1.2], [40, 70, 20, 20])
+    K = rng.uniform(70, 140, n)
+    kind = rng.integers(0, 2, n)
+    npaths = rng.choice([1, 31, 33, 257, 1000, 4099], n).astype(np.uint64)
+    opts = E.Options(K, T, kind, npaths)
+    params = E.Params(0.05, 0.03, -0.5, 2.5, 0.7, r=0.01, q=0.02)
+    cfg = E.Config(n_paths=1000, step_mode=E.STEP_GRID, seed=99)
+    p, se = engine.price(params, 100.0, opts, cfg)
+    req = E.Request(params, 100.0, opts, seed=99)
+    op, ose, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p, op, 100.0)
+    one = npaths == 1
+    assert np.all(se[one] == 0.0)
+
+
+def test_single_path_and_tiny_maturity(engine, oracle):
+    params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5)
+    opts = E.Options(np.array([0.0, 100.0, 1e6]), np.array([1e-4, 1e-4, 1e-4]), np.array([0, 1, 1]))
+    cfg = E.Config(n_paths=1, steps=1)
+    p, se = engine.price(params, 100.0, opts, cfg)
+    req = E.Request(params, 100.0, opts, seed=cfg.seed)
+    op, _, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p, op, 100.0)
+    assert p[2] == 0.0
+
+
+def test_numeric_range_error(engine):
+    params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5)
+    opts = E.Options(np.array([0.0]), 1.0, 1)
+    with pytest.raises(HexoError) as ei:
+        engine.price(params, 1e8, opts, E.Config(n_paths=64, steps=10))
+    assert ei.value.status == 6
+
+
+def test_invalid_request_errors(engine):
+    params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5)
+    with pytest.raises(HexoError) as ei:
+        engine.price(params, 100.0, E.Options(np.array([100.0]), 0.0, 0), E.Config())
+    assert ei.value.status == 1
+    with pytest.raises(HexoError):
+        engine.price(params, 100.0, E.Options(np.array([100.0]), 1.0, 0), E.Config(block=100))

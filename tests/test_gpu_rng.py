@@ -1,0 +1,81 @@
+"""GPU random numbers against the oracle, bit for bit, through the C ABI.
+
+* SHISHUA words of streams seed + k (the device generator vs the oracle's).
+* The two-buffer RNG as the path kernel runs it (shared-memory ring with a
+  warp-synchronous look-ahead block) against the oracle's restatement of the
+  reference RNG class, for draw-kind sequences with few and many uniforms.
+* AS241 of every word: the device's integer-rounded float32 evaluation
+  against the oracle's Fortran-semantics restatement, including the edge
+  words where rounding decides P = 1, |Q| = 0.425 or the far tail.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, unhex
+
+pytestmark = pytest.mark.gpu
+
+
+def test_shishua_words(engine, oracle):
+    seed, n_streams, n_words = 42, 300, 80
+    got = engine.rng_words(seed, n_streams, n_words)
+    for k in (0, 1, 7, 128, 299):
+        want = oracle.shishua_words([(seed + k) & 0xFFFFFFFF, 0, 0, 0], n_words)
+        assert np.array_equal(got[k], want), k
+
+
+def test_shishua_seed_wraps_mod_2_32(engine, oracle):
+    seed = 0xFFFFFFF0
+    got = engine.rng_words(seed, 40, 16)
+    for k in (0, 15, 16, 39):
+        want = oracle.shishua_words([(seed + k) & 0xFFFFFFFF, 0, 0, 0], 16)
+        assert np.array_equal(got[k], want), k
+
+
+@pytest.mark.parametrize("p_uniform", [0.0, 0.02, 0.3, 0.5, 1.0])
+def test_two_buffer_draws(engine, oracle, p_uniform):
+    rng = np.random.default_rng(int(p_uniform * 1000) + 1)
+    kinds = (rng.random(1500) < p_uniform).astype(np.uint8)
+    seed, n_streams = 1234, 96
+    got = engine.rng_draws(seed, n_streams, kinds)
+    for k in range(0, n_streams, 7):
+        want = oracle.rng_draws(seed + k, 16, kinds)
+        assert np.array_equal(got[k].view(np.uint64), want.view(np.uint64)), (k, p_uniform)
+
+
+def test_draws_match_reference_golden(engine):
+    for case in golden("rng_draws.json"):
+        if case["size"] != 16:
+            continue
+        got = engine.rng_draws(case["seed"], 1, np.array(case["kinds"], dtype=np.uint8))[0]
+        assert np.array_equal(got.view(np.uint64), unhex(case["draws"]).view(np.uint64)), case["seed"]
+
+
+def edge_words():
+    two64 = 1 << 64
+    w = [0, 1, 2, 3, (1 << 53) - 1, 1 << 53, (1 << 53) + 1, 1 << 63, (1 << 63) - 1, (1 << 63) + 1,
+         two64 - 1, two64 - 1024, two64 - 1025, two64 - 2048, two64 - 2049, 1 << 11, (1 << 11) + 1]
+    # around |Q| = 0.425 (P = 0.075, 0.925) and the 5.0 split of the tail (R = e^-25)
+    for p in (0.075, 0.925, np.exp(-25.0), 1 - np.exp(-25.0), 1e-15, 1 - 1e-15):
+        c = int(p * 2.0 ** 64)
+        w += [max(0, min(two64 - 1, c + d)) for d in range(-3000, 3001, 97)]
+    return np.array(w, dtype=np.uint64)
+
+
+def test_normals_edge_words(engine, oracle):
+    w = edge_words()
+    got = engine.normals(w)
+    want = oracle.normals(w)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
+def test_normals_random_words(engine, oracle):
+    rng = np.random.default_rng(77)
+    w = rng.integers(0, 2 ** 64 - 1, size=1 << 21, dtype=np.uint64, endpoint=True)
+    # also dense tails: small and large words
+    w[: 1 << 18] >>= rng.integers(3, 60, size=1 << 18).astype(np.uint64)
+    w[1 << 18: 1 << 19] = ~(w[1 << 18: 1 << 19] >> rng.integers(3, 60, size=1 << 18).astype(np.uint64))
+    got = engine.normals(w)
+    want = oracle.normals(w)
+    bad = np.flatnonzero(got.view(np.uint64) != want.view(np.uint64))
+    assert bad.size == 0, (bad[:5], w[bad[:5]], got[bad[:5]], want[bad[:5]])
