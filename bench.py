@@ -240,7 +240,8 @@ def run_engine(args, rank, world, local):
         cfg64 = W.uneven_batch(seed=2, precision=FP64)[1]
         nom64 = plan_stats(reqs[:n_fp64], cfg64).nominal_path_steps
         t0 = time.perf_counter()
-        p64 = [eng.price(rq.params, rq.S0, rq.options, cfg64) for rq in reqs[:n_fp64]]
+        # one request per launch, each on its own seed, as the batch prices it
+        p64 = [eng.price_batch([rq], cfg64)[0] for rq in reqs[:n_fp64]]
         fp64_s = time.perf_counter() - t0
         fp64_value = nom64 / fp64_s
         rel, in_se, n_big = 0.0, 0, 0

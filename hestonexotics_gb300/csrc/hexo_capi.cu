@@ -158,10 +158,14 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(db.args.acc, 0, (size_t)n_out * kLimbs * sizeof(unsigned long long), st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(db.args.queue, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(db.ev_k0, st)) != cudaSuccess) return e;
+    // inside a stream capture the timing events become event-record nodes of the graph
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(st, &cap)) != cudaSuccess) return e;
+    const unsigned rec_flags = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    if ((e = cudaEventRecordWithFlags(db.ev_k0, st, rec_flags)) != cudaSuccess) return e;
     if (db.args.n_tiles > 0)
         if ((e = launch_paths(db.f32, db.plan.shape, db.grid, db.smem, st, db.args)) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(db.ev_k1, st)) != cudaSuccess) return e;
+    if ((e = cudaEventRecordWithFlags(db.ev_k1, st, rec_flags)) != cudaSuccess) return e;
     if ((e = launch_finalize(db.args.acc, db.d_paths, db.d_disc, n_out, db.d_price, db.d_se, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_price, db.d_price, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_se, db.d_se, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;

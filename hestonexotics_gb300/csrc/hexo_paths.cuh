@@ -24,7 +24,11 @@ namespace hexo {
 
 constexpr int kPayChunk = 64;   // options reduced per CTA barrier round
 
-__device__ __forceinline__ float fsqrt_fast(float x) { return x * rsqrtf(fmaxf(x, 1e-30f)); }
+// Square root of max(x, 0) from the MUFU reciprocal square root.
+__device__ __forceinline__ float fsqrt_fast(float x) {
+    const float y = fmaxf(x, 0.0f);
+    return __fmul_rn(y, rsqrtf(fmaxf(y, 1e-30f)));
+}
 
 template <bool kF32> struct Real;
 template <> struct Real<false> { typedef double T; };
@@ -32,79 +36,100 @@ template <> struct Real<true> { typedef float T; };
 
 template <bool kF32>
 struct PathVars {
-    typename Real<kF32>::T lx, v, X, Xp, acc;  // lx: log X (FP64) or log X - log S0 (FP32)
+    typename Real<kF32>::T lx, v, X, Xp, acc;  // lx: log X (FP64); log X - log S0 - (rho/sigma) v (FP32)
 };
+
+// The path arithmetic below names every rounding (__fma_rn, __dmul_rn, ...)
+// so that the compiler cannot contract or reassociate differently in
+// different template instantiations: every launch shape computes the same
+// bits for the same path.
 
 // One QE step of one path (HSimulation.tpp:52-86), FP64.
 __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, double theta, dev::Shishua &g,
                                         dev::RngCursor &c, uint64_t *base, uint32_t stride) {
     const double v = pv.v;
-    const double m = theta + (v - theta) * sg.disc;                 // tpp:59
-    const double sp2 = fabs(v * sg.cA + sg.cB);                     // tpp:60
-    const double mm = m * m;
-    const bool quad = sp2 < 1.5 * mm;                               // Psi < PSI_C, tpp:61,63
+    const double m = __fma_rn(__dsub_rn(v, theta), sg.disc, theta);         // tpp:59
+    const double sp2 = fabs(__fma_rn(v, sg.cA, sg.cB));                      // tpp:60
+    const double mm = __dmul_rn(m, m);
+    const bool quad = sp2 < __dmul_rn(1.5, mm);                              // Psi < PSI_C, tpp:61,63
     const uint64_t w1 = quad ? dev::rng_next_g(g, c, base, stride) : dev::rng_next_u(g, c, base, stride);
     const uint64_t w2 = dev::rng_next_g(g, c, base, stride);
     const double z1 = (double)dev::as241_word(w1);
     const double z2 = (double)dev::as241_word(w2);
     double vn;
-    if (quad) {                                                     // tpp:64-68
-        const double inv = 2.0 * mm / sp2;                          // 2/Psi
-        const double bp2 = inv - 1.0 + sqrt(inv * (inv - 1.0));
-        const double b = sqrt(bp2);
-        const double a = m / (1.0 + bp2);
-        const double zb = b + z1;
-        vn = a * zb * zb;
-    } else {                                                        // tpp:70-73
-        const double Psi = sp2 / mm;
-        const double p = (Psi - 1.0) / (Psi + 1.0);
-        const double beta = 2.0 / (m * (Psi + 1.0));
+    if (quad) {                                                              // tpp:64-68
+        const double inv = __ddiv_rn(__dmul_rn(2.0, mm), sp2);               // 2/Psi
+        const double im1 = __dsub_rn(inv, 1.0);
+        const double bp2 = __dadd_rn(im1, __dsqrt_rn(__dmul_rn(inv, im1)));
+        const double b = __dsqrt_rn(bp2);
+        const double a = __ddiv_rn(m, __dadd_rn(1.0, bp2));
+        const double zb = __dadd_rn(b, z1);
+        vn = __dmul_rn(__dmul_rn(a, zb), zb);
+    } else {                                                                 // tpp:70-73
+        const double Psi = __ddiv_rn(sp2, mm);
+        const double p = __ddiv_rn(__dsub_rn(Psi, 1.0), __dadd_rn(Psi, 1.0));
+        const double beta = __ddiv_rn(2.0, __dmul_rn(m, __dadd_rn(Psi, 1.0)));
         const double U = dev::uniform_f64(w1);
-        vn = p < U ? log((1.0 - p) / (1.0 - U)) / beta : 0.0;
+        vn = p < U ? __ddiv_rn(log(__ddiv_rn(__dsub_rn(1.0, p), __dsub_rn(1.0, U))), beta) : 0.0;
     }
     pv.v = vn;
-    pv.lx = pv.lx + sg.K0 + sg.K1 * v + sg.K2 * vn + sqrt(sg.K3 * v + sg.K4 * vn) * z2;   // tpp:80
+    double t = __dadd_rn(pv.lx, sg.K0);                                     // tpp:80
+    t = __fma_rn(sg.K1, v, t);
+    t = __fma_rn(sg.K2, vn, t);
+    const double sd = __dsqrt_rn(__fma_rn(sg.K3, v, __dmul_rn(sg.K4, vn)));
+    pv.lx = __fma_rn(sd, z2, t);
     pv.Xp = pv.X;
-    pv.X = exp(pv.lx);                                              // tpp:82
+    pv.X = exp(pv.lx);                                                       // tpp:82
 }
 
 // One QE step, FP32 form: the same scheme and draws with float state.
 __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, float theta, dev::Shishua &g,
-                                        dev::RngCursor &c, uint64_t *base, uint32_t stride, float S0) {
+                                        dev::RngCursor &c, uint64_t *base, uint32_t stride, float S0, float r) {
     const float v = pv.v;
-    const float m = fmaf(v - theta, sg.f_disc, theta);
-    const float sp2 = fabsf(fmaf(v, sg.f_cA, sg.f_cB));
-    const float mm = m * m;
-    const bool quad = sp2 < 1.5f * mm;
+    const float m = __fmaf_rn(__fsub_rn(v, theta), sg.f_disc, theta);
+    const float sp2 = fabsf(__fmaf_rn(v, sg.f_cA, sg.f_cB));
+    const float mm = __fmul_rn(m, m);
+    const bool quad = sp2 < __fmul_rn(1.5f, mm);
     const uint64_t w1 = quad ? dev::rng_next_g(g, c, base, stride) : dev::rng_next_u(g, c, base, stride);
     const uint64_t w2 = dev::rng_next_g(g, c, base, stride);
     const float z1 = dev::as241_word(w1);
     const float z2 = dev::as241_word(w2);
     float vn;
     if (quad) {
-        const float inv = __fdividef(2.0f * mm, sp2);
-        const float bp2 = inv - 1.0f + fsqrt_fast(inv * (inv - 1.0f));
+        const float inv = __fdividef(__fmul_rn(2.0f, mm), sp2);
+        const float im1 = __fsub_rn(inv, 1.0f);
+        const float bp2 = __fadd_rn(im1, fsqrt_fast(__fmul_rn(inv, im1)));
         const float b = fsqrt_fast(bp2);
-        const float a = __fdividef(m, 1.0f + bp2);
-        const float zb = b + z1;
-        vn = a * zb * zb;
+        const float a = __fdividef(m, __fadd_rn(1.0f, bp2));
+        const float zb = __fadd_rn(b, z1);
+        vn = __fmul_rn(__fmul_rn(a, zb), zb);
     } else {
         const float Psi = __fdividef(sp2, mm);
-        const float p = __fdividef(Psi - 1.0f, Psi + 1.0f);
+        const float pp1 = __fadd_rn(Psi, 1.0f);
+        const float p = __fdividef(__fsub_rn(Psi, 1.0f), pp1);
         bool ovf;
         const uint64_t W = dev::rn53(w1, &ovf);                    // U = W 2^-64, 1 - U = (2^64 - W) 2^-64
-        const float U = ovf ? 1.0f : __ull2float_rn(W) * 0x1p-64f;
-        const float omU = ovf ? 0.0f : (W == 0 ? 1.0f : __ull2float_rn(0ull - W) * 0x1p-64f);
-        vn = p < U ? 0.5f * m * (Psi + 1.0f) * (__logf(__fdividef(2.0f, Psi + 1.0f)) - __logf(omU)) : 0.0f;
+        const float U = ovf ? 1.0f : __fmul_rn(__ull2float_rn(W), 0x1p-64f);
+        const float omU = ovf ? 0.0f : (W == 0 ? 1.0f : __fmul_rn(__ull2float_rn(0ull - W), 0x1p-64f));
+        // v = log((1-p)/(1-U)) / beta with 1-p = 2/(Psi+1), 1/beta = m (Psi+1) / 2; never below 0
+        const float lr = __logf(__fdividef(__fdividef(2.0f, pp1), omU));
+        vn = p < U ? fmaxf(0.0f, __fmul_rn(__fmul_rn(__fmul_rn(0.5f, m), pp1), lr)) : 0.0f;
     }
     pv.v = vn;
-    float inc = fmaf(sg.f_K1, v, sg.f_K0);
-    inc = fmaf(sg.f_K2, vn, inc);
-    inc = fmaf(fsqrt_fast(fmaf(sg.f_K3, v, sg.f_K4 * vn)), z2, inc);
-    pv.lx += inc;
+    // K1 v + K2 vn = c (v + vn) + (rho/sigma)(vn - v): the second part
+    // telescopes over the steps, so it is not accumulated in float (its
+    // rounding would add up step after step); lx = log X - log S0 - r v.
+    float inc = __fmaf_rn(sg.f_c, __fadd_rn(v, vn), sg.f_K0);
+    inc = __fmaf_rn(fsqrt_fast(__fmaf_rn(sg.f_K3, v, __fmul_rn(sg.f_K4, vn))), z2, inc);
+    pv.lx = __fadd_rn(pv.lx, inc);
     pv.Xp = pv.X;
-    pv.X = S0 * __expf(pv.lx);
+    pv.X = __fmul_rn(S0, __expf(__fmaf_rn(r, vn, pv.lx)));
 }
+
+__device__ __forceinline__ float add_r(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_r(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 template <bool kF32, int PPT, int UNROLL>
 __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
@@ -127,7 +152,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         const TileDesc td = a.tiles[tile];
         const SetDesc &S = a.sets[td.set];
         const R theta = kF32 ? (R)S.f_theta : (R)S.theta;
-        const float S0f = S.f_S0;
+        const float S0f = S.f_S0, rf = S.f_r;
 
         dev::Shishua g[PPT];
         dev::RngCursor c[PPT];
@@ -140,7 +165,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             active[p] = kpath[p] < S.n_paths;
             uint64_t *base = ring + (size_t)p * kRingSlots * kRngWords * bd + tid;
             dev::rng_start(g[p], c[p], base, bd, S.seed + (uint32_t)kpath[p]);
-            pv[p].lx = kF32 ? (R)0 : (R)S.logS0;
+            pv[p].lx = kF32 ? (R)(-(float)S.f_r * S.f_v0) : (R)S.logS0;   // FP32: log X - log S0 - (rho/sigma) v
             pv[p].v = kF32 ? (R)S.f_v0 : (R)S.v0;
             pv[p].X = kF32 ? (R)S.f_S0 : (R)S.S0;
             pv[p].Xp = pv[p].X;
@@ -157,9 +182,9 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                 for (int p = 0; p < PPT; ++p) {
                     uint64_t *base = ring + (size_t)p * kRingSlots * kRngWords * bd + tid;
                     dev::rng_topup(g[p], c[p], base, bd);
-                    if constexpr (kF32) qe_step(pv[p], sg, theta, g[p], c[p], base, bd, S0f);
+                    if constexpr (kF32) qe_step(pv[p], sg, theta, g[p], c[p], base, bd, S0f, rf);
                     else qe_step(pv[p], sg, theta, g[p], c[p], base, bd);
-                    pv[p].acc += hdt * (pv[p].X + pv[p].Xp);
+                    pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
                 }
             }
             // the pricing step
@@ -167,7 +192,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             for (int p = 0; p < PPT; ++p) {
                 uint64_t *base = ring + (size_t)p * kRingSlots * kRngWords * bd + tid;
                 dev::rng_topup(g[p], c[p], base, bd);
-                if constexpr (kF32) qe_step(pv[p], sg, theta, g[p], c[p], base, bd, S0f);
+                if constexpr (kF32) qe_step(pv[p], sg, theta, g[p], c[p], base, bd, S0f, rf);
                 else qe_step(pv[p], sg, theta, g[p], c[p], base, bd);
             }
             for (uint32_t mj = sg.mat_begin; mj < sg.mat_end; ++mj) {
@@ -177,13 +202,13 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                 for (int p = 0; p < PPT; ++p) {
                     R interp;
                     if constexpr (kF32) {
-                        interp = (pv[p].X - pv[p].Xp) * M.f_w;
-                        asian[p] = (pv[p].acc + interp) * M.f_invT;
-                    } else {
-                        interp = (pv[p].X - pv[p].Xp) * M.tmtp / M.dt;     // AsianContract.h:30-31
-                        asian[p] = (pv[p].acc + interp) / M.T;             // AsianContract.h:32
+                        interp = __fmul_rn(__fsub_rn(pv[p].X, pv[p].Xp), M.f_w);
+                        asian[p] = __fmul_rn(__fadd_rn(pv[p].acc, interp), M.f_invT);
+                    } else {                                               // AsianContract.h:30-32
+                        interp = __ddiv_rn(__dmul_rn(__dsub_rn(pv[p].X, pv[p].Xp), M.tmtp), M.dt);
+                        asian[p] = __ddiv_rn(__dadd_rn(pv[p].acc, interp), M.T);
                     }
-                    euro[p] = pv[p].Xp + interp;                           // VanillaContract.h:28-29
+                    euro[p] = add_r(pv[p].Xp, interp);                     // VanillaContract.h:28-29
                     if (a.dbg_asian != nullptr && active[p]) {
                         const size_t at = (size_t)(kpath[p] - a.dbg_lo) * a.dbg_mats + mj;
                         a.dbg_asian[at] = (double)asian[p];
@@ -201,10 +226,10 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                             if (active[p] && kpath[p] < O.n_paths) {
                                 if constexpr (kF32) {
                                     const float f = O.kind == 0 ? asian[p] : euro[p];
-                                    ok &= dev::limbs_add_f32(fmaxf(0.0f, f - O.f_strike), l);
+                                    ok &= dev::limbs_add_f32(fmaxf(0.0f, __fsub_rn(f, O.f_strike)), l);
                                 } else {
                                     const double f = O.kind == 0 ? asian[p] : euro[p];
-                                    ok &= dev::limbs_add_f64(fmax(0.0, f - O.strike), l);   // AsianContract.h:43-47
+                                    ok &= dev::limbs_add_f64(fmax(0.0, __dsub_rn(f, O.strike)), l);   // AsianContract.h:43-47
                                 }
                             }
                         }
@@ -229,7 +254,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             }
             const R hda = kF32 ? (R)sg.f_hdt_after : (R)sg.hdt_after;
 #pragma unroll
-            for (int p = 0; p < PPT; ++p) pv[p].acc += hda * (pv[p].X + pv[p].Xp);
+            for (int p = 0; p < PPT; ++p) pv[p].acc = fma_r(hda, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
         }
     }
 }

@@ -101,6 +101,7 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
         s.f_disc = (float)s.disc; s.f_cA = (float)s.cA; s.f_cB = (float)s.cB;
         s.f_K0 = (float)s.K0; s.f_K1 = (float)s.K1; s.f_K2 = (float)s.K2;
         s.f_K3 = (float)s.K3; s.f_K4 = (float)s.K4; s.f_hdt = (float)s.hdt;
+        s.f_c = (float)(0.5 * dt * (p.kappa * p.rho / p.sigma - 0.5));
         return s;
     };
     double t = 0.0;
@@ -153,6 +154,7 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
     sd.f_S0 = (float)S0;
     sd.f_v0 = (float)p.v0;
     sd.f_theta = (float)p.theta;
+    sd.f_r = (float)(p.rho / p.sigma);
     sd.seed = seed;
     sd.seg_count = (uint32_t)out.segs.size();
     sd.mat_count = (uint32_t)m;

@@ -31,6 +31,8 @@ struct SegDesc {
     double hdt_after; // 0.5 dt of the next segment: trapezoid weight after the pricing step
     // FP32 copies
     float f_disc, f_cA, f_cB, f_K0, f_K1, f_K2, f_K3, f_K4, f_hdt, f_hdt_after;
+    float f_c;      // 0.5 dt (kappa rho / sigma - 0.5): K1 = c - rho/sigma, K2 = c + rho/sigma
+    float f_pad0;
     uint32_t n_steps;   // steps in this segment, the last one prices
     uint32_t mat_begin; // maturities priced after the last step: [mat_begin, mat_end) (set-local)
     uint32_t mat_end;
@@ -57,7 +59,7 @@ struct OptDesc {
 
 struct SetDesc {
     double S0, logS0, v0, theta;
-    float f_S0, f_v0, f_theta, f_pad;
+    float f_S0, f_v0, f_theta, f_r;   // f_r = rho / sigma
     uint32_t seed;
     uint32_t seg_begin, seg_count;
     uint32_t mat_begin, mat_count;
