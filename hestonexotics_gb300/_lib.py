@@ -15,7 +15,7 @@ HEXO_LIMBS = 6
 STATUS_NAMES = {
     0: "HEXO_OK", 1: "HEXO_ERR_INVALID", 2: "HEXO_ERR_CUDA", 3: "HEXO_ERR_NOMEM",
     4: "HEXO_ERR_UNSUPPORTED", 5: "HEXO_ERR_TIMEOUT", 6: "HEXO_ERR_NUMERIC",
-    7: "HEXO_ERR_NOT_FOUND", 8: "HEXO_ERR_ADMISSION", 9: "HEXO_ERR_SHUTDOWN",
+    7: "HEXO_ERR_NOT_FOUND", 8: "HEXO_ERR_ADMISSION", 9: "HEXO_ERR_SHUTDOWN", 10: "HEXO_ERR_TOO_LARGE",
 }
 
 
@@ -107,6 +107,8 @@ PROTOTYPES = {
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
     "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.POINTER(hexo_option), C.c_uint32,
                                       C.POINTER(hexo_mc_cfg), _U64, _D, _D]),
+    "hexo_price_noalloc": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
+                                     C.POINTER(hexo_mc_cfg), _D, _D, _P]),
     "hexo_plan_stats_get": (C.c_int, [C.POINTER(hexo_request), C.c_uint32, C.POINTER(hexo_mc_cfg),
                                       C.POINTER(hexo_plan_stats)]),
     "hexo_plan_schedule": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,

@@ -230,6 +230,7 @@ const char *hexo_status_string(hexo_status s) {
     case HEXO_ERR_NOT_FOUND: return "not found";
     case HEXO_ERR_ADMISSION: return "request exceeds the device-memory cap";
     case HEXO_ERR_SHUTDOWN: return "server shut down";
+    case HEXO_ERR_TOO_LARGE: return "request exceeds the no-allocation entry point's limits";
     }
     return "unknown status";
 }

@@ -50,7 +50,8 @@ typedef enum hexo_status {
     HEXO_ERR_NUMERIC = 6,      /* a payoff was not finite or exceeded the fixed-point range */
     HEXO_ERR_NOT_FOUND = 7,    /* unknown ticket */
     HEXO_ERR_ADMISSION = 8,    /* request can never fit the device-memory cap */
-    HEXO_ERR_SHUTDOWN = 9      /* server is shutting down */
+    HEXO_ERR_SHUTDOWN = 9,     /* server is shutting down */
+    HEXO_ERR_TOO_LARGE = 10    /* request exceeds the fixed limits of hexo_price_noalloc */
 } hexo_status;
 
 const char *hexo_status_string(hexo_status s);
@@ -193,6 +194,33 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
 hexo_status hexo_finalize_limbs(const hexo_params *p, const hexo_option *opts, uint32_t n_opts,
                                 const hexo_mc_cfg *cfg, const uint64_t *limbs, double *price_out,
                                 double *stderr_out);
+
+/* ------------------------------------------------- pricing without allocation */
+
+/* No counterpart in the reference: this entry point exists for callers that
+ * cannot let a library allocate GPU memory, such as a process whose framework
+ * or serving stack has reserved nearly all device memory through its own
+ * pool (an allocation behind its back would fail or fragment that pool), or a
+ * latency-critical loop where cudaMalloc/cudaFree would add device-wide
+ * synchronisation.  It prices one request like hexo_price, with the same
+ * results bit for bit, and allocates nothing: no device memory and no host
+ * heap.  Its device-side working memory is one array of
+ * HEXO_NOALLOC_SCRATCH_BYTES compiled into the library, which every GPU that
+ * loads the library holds until the process exits.  Limits: at most
+ * HEXO_NOALLOC_MAX_OPTIONS options and HEXO_NOALLOC_MAX_PATHS paths per
+ * option; beyond them it returns HEXO_ERR_TOO_LARGE before touching the GPU.
+ * The launch shape is fixed (256 threads, one path each).  It runs on the
+ * current device and on `stream` (a cudaStream_t; NULL = the default stream)
+ * and blocks until the results are in price_out / stderr_out (host arrays of
+ * n_opts; stderr_out may be NULL).  The first call on each device looks up
+ * the array's device address, so make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (from several threads or streams) race and must be serialised. */
+#define HEXO_NOALLOC_MAX_OPTIONS 128u
+#define HEXO_NOALLOC_MAX_PATHS (1u << 20)
+#define HEXO_NOALLOC_SCRATCH_BYTES (128u << 10)
+hexo_status hexo_price_noalloc(const hexo_params *p, double S0, const hexo_option *opts, uint32_t n_opts,
+                               const hexo_mc_cfg *cfg, double *price_out, double *stderr_out, void *stream);
 
 /* ------------------------------------------------------------- planning */
 
