@@ -14,24 +14,32 @@ cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t 
     return cudaLaunchKernel(fn, dim3(grid), dim3(sh.block), params, smem, st);
 }
 
-__global__ void finalize_kernel(const unsigned long long *__restrict__ acc, const uint64_t *__restrict__ n_paths,
-                                const double *__restrict__ disc, uint32_t n, double *__restrict__ price,
-                                double *__restrict__ se) {
+// Sums the CTA-private copies of the limbs (exact integer additions) and
+// finalises each option.
+__global__ void finalize_kernel(const unsigned long long *__restrict__ acc, uint32_t n_slots, uint64_t slot_stride,
+                                const uint64_t *__restrict__ n_paths, const double *__restrict__ disc, uint32_t n,
+                                double *__restrict__ price, double *__restrict__ se,
+                                unsigned long long *__restrict__ acc_sum) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint64_t l[kLimbs];
+    uint64_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t s = 0; s < n_slots; ++s)
 #pragma unroll
-    for (int x = 0; x < kLimbs; ++x) l[x] = acc[(size_t)i * kLimbs + x];
+        for (int x = 0; x < kLimbs; ++x) l[x] += acc[(size_t)s * slot_stride + (size_t)i * kLimbs + x];
+    if (acc_sum != nullptr)
+#pragma unroll
+        for (int x = 0; x < kLimbs; ++x) acc_sum[(size_t)i * kLimbs + x] = l[x];
     double p, s;
     finalize_limbs6(l, n_paths[i], disc[i], &p, &s);
     price[i] = p;
     se[i] = s;
 }
 
-cudaError_t launch_finalize(const unsigned long long *acc, const uint64_t *n_paths, const double *disc, uint32_t n,
-                            double *price, double *se, cudaStream_t st) {
+cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
+                            const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
+                            unsigned long long *acc_sum, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_paths, disc, n, price, se);
+    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, n, price, se, acc_sum);
     return cudaGetLastError();
 }
 
@@ -58,19 +66,24 @@ __global__ void dbg_words_kernel(uint32_t seed, uint32_t n_streams, uint32_t n_w
 // The two-buffer RNG through the same ring code as the path kernel.
 __global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint64_t *ring = reinterpret_cast<uint64_t *>(smem_raw);
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t bd = blockDim.x;
-    uint64_t *base = ring + threadIdx.x;
+    const uint32_t bd = blockDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    uint64_t *raw = reinterpret_cast<uint64_t *>(smem_raw);
+    float *nrm = reinterpret_cast<float *>(raw + 2 * kRngWords * bd);
+    float *tq_r = nrm + 2 * kRngWords * bd;
+    uint16_t *tq_i = reinterpret_cast<uint16_t *>(tq_r + (bd >> 5) * 64);
+    uint8_t *tbl = reinterpret_cast<uint8_t *>(tq_i + (bd >> 5) * 64);
+    const uint32_t k = blockIdx.x * bd + tid;
+    dev::Ring r{raw + tid, nrm + tid, bd};
+    dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tbl + warp * 32, tq_r + warp * 64, tq_i + warp * 64, lane};
     dev::Shishua g;
-    dev::RngCursor c;
-    dev::rng_start(g, c, base, bd, seed + k);
+    dev::RngLane c;
+    dev::rng_start(g, c, r, ws, seed + k);
     for (uint32_t i = 0; i < n; i += 2) {
-        dev::rng_topup(g, c, base, bd);   // same cadence as one QE step (two draws)
+        dev::rng_topup(g, c, r, ws);   // same cadence as one QE step (two draws)
         for (uint32_t h = i; h < i + 2 && h < n; ++h) {
             double v;
-            if (kinds[h]) v = dev::uniform_f64(dev::rng_next_u(g, c, base, bd));
-            else v = (double)dev::as241_word(dev::rng_next_g(g, c, base, bd));
+            if (kinds[h]) v = dev::uniform_f64(dev::rng_next_u(g, c, r));
+            else v = (double)dev::rng_next_g(g, c, r);
             if (k < n_streams) out[(size_t)k * n + h] = v;
         }
     }
@@ -89,7 +102,7 @@ cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words
 cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
                              cudaStream_t st) {
     const uint32_t bd = 64;
-    const size_t smem = (size_t)kRingSlots * kRngWords * bd * sizeof(uint64_t);
+    const size_t smem = (size_t)2 * kRngWords * bd * (sizeof(uint64_t) + sizeof(float)) + (bd / 32) * (64 * 4 + 64 * 2 + 32);
     dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, n_streams, kinds, n, out);
     return cudaGetLastError();
 }

@@ -80,6 +80,10 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     hexo_status s = shape_check(ctx, f32, bp.shape, db.smem, db.ctas_per_sm);
     if (s != HEXO_OK) return s;
     const uint32_t n_out = bp.n_out;
+    db.grid = std::max<uint32_t>(1, std::min<uint32_t>(ctx->sm_count * db.ctas_per_sm, (uint32_t)bp.tiles.size()));
+    // one private copy of the sums per CTA, within a 256 MiB budget
+    const uint64_t per_slot = std::max<uint64_t>(1, (uint64_t)n_out * kLimbs * sizeof(unsigned long long));
+    db.n_slots = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(db.grid, (256ull << 20) / per_slot));
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     const size_t o_sets = take(bp.sets.size() * sizeof(SetDesc));
@@ -89,7 +93,8 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_tiles = take(std::max<size_t>(1, bp.tiles.size()) * sizeof(TileDesc));
     const size_t o_paths = take(n_out * sizeof(uint64_t));
     const size_t o_disc = take(n_out * sizeof(double));
-    const size_t o_acc = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
+    const size_t o_acc = take((size_t)db.n_slots * n_out * kLimbs * sizeof(unsigned long long));
+    const size_t o_acc_sum = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_price = take(n_out * sizeof(double));
     const size_t o_se = take(n_out * sizeof(double));
     const size_t o_ctl = take(2 * sizeof(uint32_t));   // queue head, error flags
@@ -120,6 +125,9 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     a.tiles = reinterpret_cast<const TileDesc *>(d + o_tiles);
     a.n_tiles = (uint32_t)bp.tiles.size();
     a.acc = reinterpret_cast<unsigned long long *>(d + o_acc);
+    a.n_slots = db.n_slots;
+    a.acc_slot_stride = (uint64_t)n_out * kLimbs;
+    db.d_acc_sum = reinterpret_cast<unsigned long long *>(d + o_acc_sum);
     a.queue = reinterpret_cast<unsigned int *>(d + o_ctl);
     a.error = reinterpret_cast<int *>(d + o_ctl + sizeof(uint32_t));
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
@@ -147,8 +155,6 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
                    bp.tiles.size() * sizeof(TileDesc) + n_out * (sizeof(uint64_t) + sizeof(double));
     if ((e = cudaEventCreate(&db.ev_k0)) != cudaSuccess || (e = cudaEventCreate(&db.ev_k1)) != cudaSuccess)
         return cuda_fail(ctx, e, "cudaEventCreate");
-    const uint32_t slots = ctx->sm_count * db.ctas_per_sm;
-    db.grid = std::max<uint32_t>(1, std::min<uint32_t>(slots, (uint32_t)bp.tiles.size()));
     return HEXO_OK;
 }
 
@@ -156,7 +162,9 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
 cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     const uint32_t n_out = db.plan.n_out;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(db.args.acc, 0, (size_t)n_out * kLimbs * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(db.args.acc, 0, (size_t)db.n_slots * n_out * kLimbs * sizeof(unsigned long long), st)) !=
+        cudaSuccess)
+        return e;
     if ((e = cudaMemsetAsync(db.args.queue, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return e;
     // inside a stream capture the timing events become event-record nodes of the graph
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -166,11 +174,13 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     if (db.args.n_tiles > 0)
         if ((e = launch_paths(db.f32, db.plan.shape, db.grid, db.smem, st, db.args)) != cudaSuccess) return e;
     if ((e = cudaEventRecordWithFlags(db.ev_k1, st, rec_flags)) != cudaSuccess) return e;
-    if ((e = launch_finalize(db.args.acc, db.d_paths, db.d_disc, n_out, db.d_price, db.d_se, st)) != cudaSuccess) return e;
+    if ((e = launch_finalize(db.args.acc, db.n_slots, db.args.acc_slot_stride, db.d_paths, db.d_disc, n_out,
+                             db.d_price, db.d_se, db.d_acc_sum, st)) != cudaSuccess)
+        return e;
     if ((e = cudaMemcpyAsync(db.h_price, db.d_price, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_se, db.d_se, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if (copy_acc)
-        if ((e = cudaMemcpyAsync(db.h_acc, db.args.acc, (size_t)n_out * kLimbs * sizeof(unsigned long long),
+        if ((e = cudaMemcpyAsync(db.h_acc, db.d_acc_sum, (size_t)n_out * kLimbs * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     return cudaMemcpyAsync(db.h_ctl, db.args.queue, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
 }

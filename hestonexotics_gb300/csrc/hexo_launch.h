@@ -7,10 +7,14 @@
 
 namespace hexo {
 
-// Dynamic shared memory of the path kernel: the RNG rings plus the payoff
-// reduction scratch.
+// Dynamic shared memory of the path kernel: per path two raw slots (16 x u64)
+// and two normal slots (16 x f32); per warp the conversion tables (64 queued
+// tail inputs and items, 32 lane entries); the 64-option staging window of
+// the payoff sums (16-byte aligned).
 inline size_t paths_smem_bytes(uint32_t block, uint32_t ppt) {
-    return (size_t)ppt * kRingSlots * kRngWords * block * sizeof(uint64_t) + 64u * kLimbs * sizeof(unsigned long long);
+    const size_t rings = (size_t)ppt * 2 * kRngWords * block * (sizeof(uint64_t) + sizeof(float)) +
+                         (size_t)(block / 32) * (64 * 4 + 64 * 2 + 32);
+    return (rings + 15) / 16 * 16 + 64u * kLimbs * sizeof(unsigned long long);
 }
 
 // nullptr when (ppt, unroll) is not instantiated.
@@ -22,9 +26,11 @@ inline const void *paths_kernel_ptr(bool f32, uint32_t ppt, uint32_t unroll) {
 cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t smem, cudaStream_t st,
                          const KernelArgs &a);
 
-// Finaliser: price and standard error per output slot from the limb sums.
-cudaError_t launch_finalize(const unsigned long long *acc, const uint64_t *n_paths, const double *disc, uint32_t n,
-                            double *price, double *se, cudaStream_t st);
+// Finaliser: sums the n_slots private copies of the limbs (acc_sum, when not
+// null, receives the totals) and writes price and standard error per slot.
+cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
+                            const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
+                            unsigned long long *acc_sum, cudaStream_t st);
 
 // Debug kernels.
 cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st);

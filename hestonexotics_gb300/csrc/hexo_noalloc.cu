@@ -118,6 +118,10 @@ SegDesc na_segment(const hexo_params &p, double dt) {
     s.f_K0 = (float)s.K0; s.f_K1 = (float)s.K1; s.f_K2 = (float)s.K2;
     s.f_K3 = (float)s.K3; s.f_K4 = (float)s.K4; s.f_hdt = (float)s.hdt;
     s.f_c = (float)(0.5 * dt * (p.kappa * p.rho / p.sigma - 0.5));
+    ds_split(s.disc, s.ds_disc);
+    ds_split(p.theta * (1.0 - s.disc), s.ds_m0);
+    ds_split(s.cA, s.ds_cA);
+    ds_split(s.cB, s.ds_cB);
     return s;
 }
 
@@ -241,6 +245,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     sd.f_v0 = (float)p.v0;
     sd.f_theta = (float)p.theta;
     sd.f_r = (float)(p.rho / p.sigma);
+    ds_split(p.v0, sd.ds_v0);
     sd.seed = cfg->seed;
     sd.seg_count = n_segs;
     sd.mat_count = m;
@@ -292,6 +297,8 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     a.tiles = reinterpret_cast<const TileDesc *>(base + kOffTiles);
     a.n_tiles = n_tiles;
     a.acc = reinterpret_cast<unsigned long long *>(base + kOffAcc);
+    a.n_slots = 1;
+    a.acc_slot_stride = (uint64_t)n_opts * kLimbs;
     a.queue = reinterpret_cast<unsigned int *>(base + kOffCtl);
     a.error = reinterpret_cast<int *>(base + kOffCtl + sizeof(uint32_t));
     const LaunchShape sh{kNaBlock, 1, 1};
@@ -300,8 +307,8 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     double *d_price = reinterpret_cast<double *>(base + kOffPrice);
     double *d_se = reinterpret_cast<double *>(base + kOffSe);
     if (e == cudaSuccess)
-        e = launch_finalize(a.acc, reinterpret_cast<const uint64_t *>(base + kOffPaths),
-                            reinterpret_cast<const double *>(base + kOffDisc), n_opts, d_price, d_se, s);
+        e = launch_finalize(a.acc, 1, a.acc_slot_stride, reinterpret_cast<const uint64_t *>(base + kOffPaths),
+                            reinterpret_cast<const double *>(base + kOffDisc), n_opts, d_price, d_se, nullptr, s);
     uint32_t ctl[2] = {0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(price_out, d_price, n_opts * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && stderr_out)

@@ -102,6 +102,10 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
         s.f_K0 = (float)s.K0; s.f_K1 = (float)s.K1; s.f_K2 = (float)s.K2;
         s.f_K3 = (float)s.K3; s.f_K4 = (float)s.K4; s.f_hdt = (float)s.hdt;
         s.f_c = (float)(0.5 * dt * (p.kappa * p.rho / p.sigma - 0.5));
+        ds_split(s.disc, s.ds_disc);
+        ds_split(p.theta * (1.0 - s.disc), s.ds_m0);
+        ds_split(s.cA, s.ds_cA);
+        ds_split(s.cB, s.ds_cB);
         return s;
     };
     double t = 0.0;
@@ -155,6 +159,7 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
     sd.f_v0 = (float)p.v0;
     sd.f_theta = (float)p.theta;
     sd.f_r = (float)(p.rho / p.sigma);
+    ds_split(p.v0, sd.ds_v0);
     sd.seed = seed;
     sd.seg_count = (uint32_t)out.segs.size();
     sd.mat_count = (uint32_t)m;

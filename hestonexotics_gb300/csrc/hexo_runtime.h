@@ -22,7 +22,8 @@ struct DeviceBatch {
     BatchPlan plan;
     bool f32 = false;
     size_t smem = 0;
-    uint32_t ctas_per_sm = 0, grid = 0;
+    uint32_t ctas_per_sm = 0, grid = 0, n_slots = 1;
+    unsigned long long *d_acc_sum = nullptr;   // totals of the private sum copies
     void *dmem = nullptr;
     size_t bytes = 0;
     void *hmem = nullptr;

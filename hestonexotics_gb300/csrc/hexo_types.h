@@ -33,6 +33,8 @@ struct SegDesc {
     float f_disc, f_cA, f_cB, f_K0, f_K1, f_K2, f_K3, f_K4, f_hdt, f_hdt_after;
     float f_c;      // 0.5 dt (kappa rho / sigma - 0.5): K1 = c - rho/sigma, K2 = c + rho/sigma
     float f_pad0;
+    // double-single (hi, lo) copies for the FP32 form's variance: m = v disc + m0, s^2 = v cA + cB
+    float ds_disc[2], ds_m0[2], ds_cA[2], ds_cB[2];
     uint32_t n_steps;   // steps in this segment, the last one prices
     uint32_t mat_begin; // maturities priced after the last step: [mat_begin, mat_end) (set-local)
     uint32_t mat_end;
@@ -60,6 +62,8 @@ struct OptDesc {
 struct SetDesc {
     double S0, logS0, v0, theta;
     float f_S0, f_v0, f_theta, f_r;   // f_r = rho / sigma
+    float ds_v0[2];                   // v0 in double-single (FP32 form)
+    float f_pad1[2];
     uint32_t seed;
     uint32_t seg_begin, seg_count;
     uint32_t mat_begin, mat_count;
@@ -74,6 +78,12 @@ struct TileDesc {
     uint32_t seg_count;  // segments this block must run (to its last maturity)
 };
 
+// hi + lo float pair of a double (host side; the double-single constants)
+inline void ds_split(double x, float out[2]) {
+    out[0] = (float)x;
+    out[1] = (float)(x - (double)out[0]);
+}
+
 struct KernelArgs {
     const SetDesc *sets;
     const SegDesc *segs;     // global arrays; set-local indices are offset by SetDesc
@@ -81,8 +91,9 @@ struct KernelArgs {
     const OptDesc *opts;
     const TileDesc *tiles;
     uint32_t n_tiles;
-    uint32_t pad;
-    unsigned long long *acc; // [out_index * kLimbs + limb]
+    uint32_t n_slots;        // private copies of the sums: CTA b adds into copy b % n_slots
+    unsigned long long *acc; // [slot * acc_slot_stride + out_index * kLimbs + limb]
+    uint64_t acc_slot_stride;
     unsigned int *queue;     // [0] tile queue head
     int *error;              // [0] error flags (bit 0: non-finite payoff, bit 1: fixed-point range)
     double *dbg_asian;       // optional per-path final values (debug): [(k - dbg_lo) * dbg_mats + j]
