@@ -16,6 +16,9 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              sets, and the FP32 form's error against it
   roofline   the path kernel's algorithmic FP32-pipe operations per second
              against this GPU's measured FP32-FMA lane rate
+  serving    Poisson request streams through the continuous-batching server
+             (FP32), p50/p99 submit-to-completion latency, against the same
+             streams priced one request per plain FP64 launch
   cpu_baseline / --impl reference
              the oracle port of the reference's CPU path (OpenMP over all
              host cores) on a bounded sample of the same workload
@@ -164,6 +167,63 @@ def _oracle_price_fast(O, rq, cfg, threads):
     return price, se, limbs
 
 
+# -------------------------------------------------------------- serving
+
+def _pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if xs else None
+
+
+def run_serving(eng, rates, duration_s, fp64_rates):
+    """Open-loop Poisson request streams (workloads.request_stream) against
+    the continuous-batching server (FP32 form), and the same streams priced
+    one request per launch in the plain FP64 form, first come first served.
+    Latency is submit (arrival) to completion."""
+    from hestonexotics_gb300 import FP64
+    from hestonexotics_gb300 import workloads as W
+    from hestonexotics_gb300._lib import HEXO_OK
+    out = []
+    for rate in rates:
+        arrivals, cfg = W.request_stream(rate, duration_s, seed=3)
+        row = {"rate_per_s": rate, "requests": len(arrivals), "seconds": duration_s}
+        srv = eng.server(cfg, max_batch_requests=64, max_inflight=3)
+        prepared = [srv.prepare(a.request) for a in arrivals]
+        tickets = []
+        t0 = time.perf_counter()
+        for a, pr in zip(arrivals, prepared):
+            d = t0 + a.t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets.append(srv.submit_prepared(pr))
+        ok = 0
+        for t in tickets:
+            try:
+                srv.wait(t)
+                ok += 1
+            except Exception:
+                pass
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        row["server_fp32"] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                              "completed": ok, "launches": st["batches"], "queued_max": st["queued_max"],
+                              "mem_peak_bytes": st["mem_peak"],
+                              "path_steps_per_s": st["nominal_path_steps"] / wall}
+        if rate in fp64_rates:
+            cfg64 = type(cfg)(**{**cfg.__dict__, "precision": FP64})
+            lat = []
+            t0 = time.perf_counter()
+            for a in arrivals:
+                d = t0 + a.t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                eng.price_batch([a.request], cfg64)
+                lat.append((time.perf_counter() - (t0 + a.t)) * 1e3)
+            row["plain_fp64_one_per_launch"] = {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+                                                "mean_ms": float(np.mean(lat)), "completed": len(lat)}
+        out.append(row)
+    return out
+
+
 # -------------------------------------------------------------- engine arm
 
 def run_engine(args, rank, world, local):
@@ -266,8 +326,12 @@ def run_engine(args, rank, world, local):
                 profile_traffic = d["dram_bytes_per_path_step"] * nominal
             except (ValueError, KeyError):
                 profile_traffic = None
+        serving = None
+        if args.serve_rates:
+            rates = [float(x) for x in args.serve_rates.split(",") if x]
+            fp64_rates = [float(x) for x in args.serve_fp64_rates.split(",") if x]
+            serving = run_serving(eng, rates, args.serve_seconds, fp64_rates)
         cpu = run_cpu_baseline(rank)
-        step_sorted = sorted(step_ms)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -293,6 +357,7 @@ def run_engine(args, rank, world, local):
                          "peak_source": "FP32-FMA lane rate measured in this run by hexo_debug_pipe_peaks",
                          "alg_ops_per_path_step": ALG_FP32_OPS_PER_PATH_STEP, "kernel_ms": kms,
                          "pipe_peaks_lane_ops_per_s": peaks},
+            "serving": serving,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": (args.steps) * 2,
@@ -329,6 +394,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--fp64-sets", type=int, default=2)
+    ap.add_argument("--serve-rates", default="50,200,500,2000", help="request rates of the serving leg ('' = skip)")
+    ap.add_argument("--serve-fp64-rates", default="50,200", help="rates also priced one request per FP64 launch")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

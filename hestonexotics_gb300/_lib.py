@@ -11,6 +11,10 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libhexo_mc.so"
 
 HEXO_OK = 0
+HEXO_ERR_TIMEOUT = 5
+HEXO_ERR_NOT_FOUND = 7
+HEXO_ERR_ADMISSION = 8
+HEXO_ERR_SHUTDOWN = 9
 HEXO_LIMBS = 6
 STATUS_NAMES = {
     0: "HEXO_OK", 1: "HEXO_ERR_INVALID", 2: "HEXO_ERR_CUDA", 3: "HEXO_ERR_NOMEM",
@@ -81,6 +85,19 @@ class hexo_tune_entry(C.Structure):
                 ("ms", C.c_float)]
 
 
+class hexo_server_opts(C.Structure):
+    _fields_ = [("cfg", hexo_mc_cfg), ("mem_cap_bytes", C.c_uint64), ("max_batch_requests", C.c_uint32),
+                ("max_inflight", C.c_uint32)]
+
+
+class hexo_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("failed", C.c_uint64), ("batches", C.c_uint64), ("queued_now", C.c_uint64),
+                ("queued_max", C.c_uint64), ("inflight_now", C.c_uint64), ("mem_in_use", C.c_uint64),
+                ("mem_peak", C.c_uint64), ("nominal_path_steps", C.c_uint64), ("busy_seconds", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _U64 = C.POINTER(C.c_uint64)
@@ -103,6 +120,12 @@ PROTOTYPES = {
     "hexo_batch_collect": (C.c_int, [_P]),
     "hexo_batch_info_get": (C.c_int, [_P, C.POINTER(hexo_batch_info)]),
     "hexo_batch_destroy": (C.c_int, [_P]),
+    "hexo_server_create": (C.c_int, [_P, C.POINTER(hexo_server_opts), C.POINTER(_P)]),
+    "hexo_server_submit": (C.c_int, [_P, C.POINTER(hexo_request), _U64]),
+    "hexo_server_poll": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_int)]),
+    "hexo_server_wait": (C.c_int, [_P, C.c_uint64, C.c_uint32]),
+    "hexo_server_stats_get": (C.c_int, [_P, C.POINTER(hexo_server_stats)]),
+    "hexo_server_destroy": (C.c_int, [_P]),
     "hexo_price_partial": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
     "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.POINTER(hexo_option), C.c_uint32,

@@ -64,8 +64,8 @@ DeviceBatch::~DeviceBatch() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (ev_k0) cudaEventDestroy(ev_k0);
     if (ev_k1) cudaEventDestroy(ev_k1);
-    if (dmem) cudaFree(dmem);
-    if (hmem) cudaFreeHost(hmem);
+    if (dmem && own_d) cudaFree(dmem);
+    if (hmem && own_h) cudaFreeHost(hmem);
 }
 
 namespace {
@@ -74,6 +74,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch &db) {
     db.ctx = ctx;
+    if (db.stream == nullptr) db.stream = ctx->stream;
     db.f32 = f32;
     db.plan = std::move(plan);
     BatchPlan &bp = db.plan;
@@ -99,16 +100,27 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_se = take(n_out * sizeof(double));
     const size_t o_ctl = take(2 * sizeof(uint32_t));   // queue head, error flags
     db.bytes = off;
-    cudaError_t e = cudaMalloc(&db.dmem, db.bytes);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc batch");
+    cudaError_t e = cudaSuccess;
+    if (db.dmem == nullptr || db.dcap < db.bytes) {
+        db.dmem = nullptr;
+        db.own_d = true;
+        e = cudaMalloc(&db.dmem, db.bytes);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc batch");
+        db.dcap = db.bytes;
+    }
     // pinned host mirror of outputs: price, se, acc, ctl
     size_t hoff = 0;
     const size_t h_price = hoff; hoff = align_up(hoff + n_out * sizeof(double), 64);
     const size_t h_se = hoff; hoff = align_up(hoff + n_out * sizeof(double), 64);
     const size_t h_acc = hoff; hoff = align_up(hoff + (size_t)n_out * kLimbs * sizeof(unsigned long long), 64);
     const size_t h_ctl = hoff; hoff = align_up(hoff + 2 * sizeof(uint32_t), 64);
-    e = cudaMallocHost(&db.hmem, hoff);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMallocHost batch");
+    if (db.hmem == nullptr || db.hcap < hoff) {
+        db.hmem = nullptr;
+        db.own_h = true;
+        e = cudaMallocHost(&db.hmem, hoff);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMallocHost batch");
+        db.hcap = hoff;
+    }
     char *d = static_cast<char *>(db.dmem);
     char *h = static_cast<char *>(db.hmem);
     db.h_price = reinterpret_cast<double *>(h + h_price);
@@ -135,7 +147,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     db.d_price = reinterpret_cast<double *>(d + o_price);
     db.d_se = reinterpret_cast<double *>(d + o_se);
 
-    cudaStream_t st = ctx->stream;
+    cudaStream_t st = db.stream;
     auto up = [&](size_t o, const void *src, size_t bytes) -> cudaError_t {
         if (bytes == 0) return cudaSuccess;
         return cudaMemcpyAsync(d + o, src, bytes, cudaMemcpyHostToDevice, st);
@@ -186,7 +198,7 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
 }
 
 hexo_status batch_wait(DeviceBatch &db) {
-    cudaError_t e = cudaStreamSynchronize(db.ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(db.stream);
     if (e != cudaSuccess) return cuda_fail(db.ctx, e, "batch run");
     if (db.h_ctl[1] != 0u)
         return ctx_fail(db.ctx, HEXO_ERR_NUMERIC, "a payoff was not finite or outside the fixed-point range [0, 2^23)");

@@ -19,6 +19,7 @@ struct DevBuf {
 // Planned batch resident on the device, with pinned host mirrors of its outputs.
 struct DeviceBatch {
     hexo_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;   // the context's stream unless set before upload
     BatchPlan plan;
     bool f32 = false;
     size_t smem = 0;
@@ -27,6 +28,10 @@ struct DeviceBatch {
     void *dmem = nullptr;
     size_t bytes = 0;
     void *hmem = nullptr;
+    // Memory handed in before upload is reused when large enough (own_* false:
+    // the batch does not free it); otherwise the upload allocates its own.
+    size_t dcap = 0, hcap = 0;
+    bool own_d = true, own_h = true;
     KernelArgs args{};
     uint64_t *d_paths = nullptr;
     double *d_disc = nullptr, *d_price = nullptr, *d_se = nullptr;

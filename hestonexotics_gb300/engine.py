@@ -77,16 +77,17 @@ class Options:
     def __len__(self):
         return int(self.strike.shape[0])
 
+    _DTYPE = np.dtype([("strike", "<f8"), ("T", "<f8"), ("payoff", "<u4"), ("reserved", "<u4"),
+                       ("n_paths", "<u8")])
+
     def c_array(self):
         n = len(self)
-        arr = (L.hexo_option * max(n, 1))()
-        for i in range(n):
-            arr[i].strike = float(self.strike[i])
-            arr[i].T = float(self.T[i])
-            arr[i].payoff = int(self.payoff[i])
-            arr[i].reserved = 0
-            arr[i].n_paths = int(self.n_paths[i])
-        return arr
+        rec = np.zeros(max(n, 1), dtype=self._DTYPE)
+        rec["strike"][:n] = self.strike
+        rec["T"][:n] = self.T
+        rec["payoff"][:n] = self.payoff
+        rec["n_paths"][:n] = self.n_paths
+        return (L.hexo_option * max(n, 1)).from_buffer(rec)   # the ctypes array keeps rec alive
 
 
 @dataclass
@@ -130,6 +131,82 @@ class Batch:
         if self.handle:
             L.load().hexo_batch_destroy(self.handle)
             self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching server on an engine's context (hexo_server_*).
+
+    ``submit`` queues a request and returns a ticket at once; ``wait`` blocks
+    until that request is priced and returns its (price, stderr) arrays."""
+
+    def __init__(self, engine: "Engine", cfg: Config, mem_cap_bytes: int = 0, max_batch_requests: int = 0,
+                 max_inflight: int = 0):
+        self.engine = engine
+        self._lib = engine._lib
+        opts = L.hexo_server_opts(cfg.c(), mem_cap_bytes, max_batch_requests, max_inflight)
+        self.handle = C.c_void_p()
+        engine._check(self._lib.hexo_server_create(engine._ctx, C.byref(opts), C.byref(self.handle)))
+        self._pending = {}   # ticket -> (keep-alive objects, outputs)
+
+    def prepare(self, rq: Request):
+        """Marshals a request ahead of time; pass the result to submit_prepared."""
+        return self.engine._requests([rq])
+
+    def submit(self, rq: Request) -> int:
+        return self.submit_prepared(self.prepare(rq))
+
+    def submit_prepared(self, prepared) -> int:
+        arr, keep, outputs = prepared
+        t = C.c_uint64()
+        st = self._lib.hexo_server_submit(self.handle, arr, C.byref(t))
+        if st != L.HEXO_OK:
+            raise L.HexoError(st, "hexo_server_submit failed")
+        self._pending[t.value] = (keep, outputs[0])
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        done = C.c_int()
+        st = self._lib.hexo_server_poll(self.handle, ticket, C.byref(done))
+        if done.value:
+            self._finish(ticket, st)
+        elif st != L.HEXO_OK:
+            raise L.HexoError(st, "hexo_server_poll failed")
+        return bool(done.value)
+
+    def wait(self, ticket: int, timeout_ms: int = 600_000):
+        st = self._lib.hexo_server_wait(self.handle, ticket, timeout_ms)
+        return self._finish(ticket, st)
+
+    def _finish(self, ticket: int, st: int):
+        if st == L.HEXO_ERR_TIMEOUT:
+            raise L.HexoError(st, "request still running")
+        keep, out = self._pending.pop(ticket, (None, None))
+        if st != L.HEXO_OK:
+            raise L.HexoError(st, "request failed")
+        return out
+
+    def stats(self) -> dict:
+        s = L.hexo_server_stats()
+        self.engine._check(self._lib.hexo_server_stats_get(self.handle, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in L.hexo_server_stats._fields_}
+
+    def close(self):
+        if self.handle:
+            self._lib.hexo_server_destroy(self.handle)
+            self.handle = None
+            self._pending.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:
@@ -214,6 +291,9 @@ class Engine:
         h = C.c_void_p()
         self._check(self._lib.hexo_batch_prepare(self._ctx, arr, len(requests), C.byref(c), C.byref(h)))
         return Batch(self, h, keep, outputs)
+
+    def server(self, cfg: Config, **kw) -> Server:
+        return Server(self, cfg, **kw)
 
     def partial(self, params: Params, S0: float, options: Options, cfg: Config, path_lo: int, path_hi: int):
         n = len(options)

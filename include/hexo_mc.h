@@ -12,8 +12,8 @@
  *
  * Everything crosses as plain pointers and sizes.  Buffers are owned by the
  * caller; no call keeps a pointer after it returns, except the serving
- * requests, whose option array and output arrays must stay valid until the
- * request completes.  Errors are status codes, never exceptions; a
+ * requests, whose output arrays must stay valid until the request
+ * completes.  Errors are status codes, never exceptions; a
  * message for the last failure of a context is available from
  * hexo_ctx_last_error().  include/hexo/reference_compat.h wraps this ABI
  * in the reference's own C++ signature.
@@ -177,6 +177,53 @@ hexo_status hexo_batch_launch(hexo_batch *b);
 hexo_status hexo_batch_collect(hexo_batch *b);
 hexo_status hexo_batch_info_get(hexo_batch *b, hexo_batch_info *info);
 hexo_status hexo_batch_destroy(hexo_batch *b);
+
+/* -------------------------------------------------------------- serving */
+
+/* A continuous-batching pricing server on one context.  No counterpart in
+ * the reference (whose only pricing call is the blocking HSimulation::price,
+ * src/inc/HSimulation.h:44-96); it exists so that a calibration or quoting
+ * service can keep many small requests in flight at once.  Requests are
+ * admitted first come, first served while the device memory of the launches
+ * in flight stays under mem_cap_bytes; every admitted request joins the next
+ * persistent launch, and up to max_inflight launches run at once, each on
+ * its own stream.  A request's prices do not depend on what it was batched
+ * with: path k of a request always draws from RNG(16, seed + k), and sums are
+ * exact integers, so results equal those of hexo_price_batch for the request
+ * alone, bit for bit. */
+typedef struct hexo_server hexo_server;
+
+typedef struct hexo_server_opts {
+    hexo_mc_cfg cfg;               /* paths-per-option default, stepping, precision, ... */
+    uint64_t mem_cap_bytes;        /* device memory of launches in flight; 0 = the context's cap */
+    uint32_t max_batch_requests;   /* requests per launch; 0 = 64 */
+    uint32_t max_inflight;         /* launches in flight (streams); 0 = 2, at most 16 */
+} hexo_server_opts;
+
+typedef struct hexo_server_stats {
+    uint64_t submitted, admitted, completed, failed;
+    uint64_t batches;              /* launches made */
+    uint64_t queued_now, queued_max, inflight_now;
+    uint64_t mem_in_use, mem_peak; /* admitted device bytes (planner estimate) */
+    uint64_t nominal_path_steps;   /* of completed requests */
+    double busy_seconds;           /* wall time with at least one launch in flight */
+    double p50_ms, p99_ms, mean_ms;/* submit-to-completion latency of completed requests */
+} hexo_server_stats;
+
+hexo_status hexo_server_create(hexo_ctx *ctx, const hexo_server_opts *opts, hexo_server **out);
+/* Queues a request and returns at once with its ticket.  The options are
+ * copied; price_out / stderr_out must stay valid until the request is done. */
+hexo_status hexo_server_submit(hexo_server *s, const hexo_request *req, uint64_t *ticket);
+/* done = 1 once the request finished; the return value is then its status.
+ * A finished request is reported once (by poll or wait) and then forgotten:
+ * later calls with its ticket return HEXO_ERR_NOT_FOUND. */
+hexo_status hexo_server_poll(hexo_server *s, uint64_t ticket, int *done);
+/* Waits up to timeout_ms for the request; HEXO_ERR_TIMEOUT if still running. */
+hexo_status hexo_server_wait(hexo_server *s, uint64_t ticket, uint32_t timeout_ms);
+hexo_status hexo_server_stats_get(hexo_server *s, hexo_server_stats *out);
+/* Finishes every queued and running request, then stops; later submits
+ * from other threads get HEXO_ERR_SHUTDOWN. */
+hexo_status hexo_server_destroy(hexo_server *s);
 
 /* --------------------------------------------------------------- shards */
 
