@@ -236,7 +236,7 @@ def run_engine(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     eng = Engine(local)
-    reqs, cfg = W.uneven_batch(seed=2 + rank, precision=FP32)
+    reqs, cfg = W.uneven_batch(seed=2 + rank, precision=FP32, path_scale=args.path_scale)
     batch = eng.prepare_batch(reqs, cfg)
     info = batch.info()
     stream = torch.cuda.ExternalStream(eng.stream)
@@ -337,7 +337,8 @@ def run_engine(args, rank, world, local):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f32 AS241, exact integer sums, f64 finalise",
             "data": "synthetic (seeded uneven 64-set batch; the reference prices live option chains)",
-            "config": {"workload": WORKLOAD, "sets": len(reqs), "options": info["n_options"],
+            "config": {"workload": WORKLOAD if args.path_scale == 1.0 else f"{WORKLOAD}_paths_x{args.path_scale:g}",
+                       "sets": len(reqs), "options": info["n_options"],
                        "paths": info["n_paths"], "nominal_path_steps": nominal,
                        "executed_path_steps": info["executed_path_steps"], "tiles": info["n_tiles"],
                        "block": info["block"], "paths_per_thread": info["paths_per_thread"],
@@ -397,6 +398,8 @@ def main():
     ap.add_argument("--serve-rates", default="50,200,500,2000", help="request rates of the serving leg ('' = skip)")
     ap.add_argument("--serve-fp64-rates", default="50,200", help="rates also priced one request per FP64 launch")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--path-scale", type=float, default=1.0,
+                    help="scales every path count of the batch (1.0 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -159,3 +159,44 @@ def price_reference_partition(params7, S0, strike, T, kind, steps, n_sims, *, n_
     if n < 0:
         raise ValueError("oracle_price_reference_partition failed")
     return out, int(n)
+
+
+# ------------------------------------------------------------------ SWIFT
+
+SWIFT_TRUNCATION_RELEASE = 1e-7   # FASTMATH build (Makefile.am:67, SWIFT.cpp:12-16)
+
+
+def swift_params(params5, tau, r, S, K_min, K_max, trunc_precision=SWIFT_TRUNCATION_RELEASE) -> np.ndarray:
+    """Dynamic wavelet parameters {m, 2^m, sqrt 2^m, lower, upper, k1, k2, J} (SWIFT.cpp:21-35)."""
+    p = np.ascontiguousarray(params5, dtype=np.float64)
+    out = np.zeros(8)
+    rc = lib().oracle_swift_params(_p(p), C.c_double(tau), C.c_double(r), C.c_double(S), C.c_double(K_min),
+                                   C.c_double(K_max), C.c_double(trunc_precision), _p(out))
+    if rc != 0:
+        raise RuntimeError("swift parameters did not converge")
+    return out
+
+
+def swift_price(params5, tau, r, S, strikes, sp8=None, grad=False):
+    """European call prices of one expiry by the SWIFT restatement; with
+    grad=True also the [n, 5] gradient in (v0, vm, rho, kappa, sigma) order."""
+    strikes = np.ascontiguousarray(strikes, dtype=np.float64)
+    p = np.ascontiguousarray(params5, dtype=np.float64)
+    if sp8 is None:
+        sp8 = swift_params(p, tau, r, S, strikes.min(), strikes.max())
+    sp8 = np.ascontiguousarray(sp8, dtype=np.float64)
+    n = len(strikes)
+    price = np.zeros(n)
+    g = np.zeros(5 * n) if grad else None
+    rc = lib().oracle_swift_price(_p(p), C.c_double(tau), C.c_double(r), C.c_double(S), _p(strikes), C.c_uint32(n),
+                                  _p(sp8), _p(price), _p(g) if grad else None)
+    if rc != 0:
+        raise RuntimeError("swift pricing failed")
+    return (price, g.reshape(n, 5)) if grad else price
+
+
+def heston_chf_grad(params5, tau, u: complex) -> np.ndarray:
+    p = np.ascontiguousarray(params5, dtype=np.float64)
+    out = np.zeros(12)
+    lib().oracle_heston_chf_grad(_p(p), C.c_double(tau), C.c_double(u.real), C.c_double(u.imag), _p(out))
+    return out[0::2] + 1j * out[1::2]

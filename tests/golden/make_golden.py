@@ -11,15 +11,21 @@ SHISHUA and AS241 restatement; see oracle/Makefile) and records
                       OpenMP thread (the reference's own stream partition)
   ref_paths.json      per-path payoffs through the reference's HQEAnderson and
                       contract classes with one RNG(16, seed + k) per path
+  swift_golden.json   the SWIFT known answers of the reference's unit tests,
+                      read as text from src/UnitTest.cpp: inputs (:155-181),
+                      the 40 prices of pricing_test (:221-261) and the 200
+                      gradient entries of gradient_test (:278-478) with its
+                      component map (:479)
 
 Floats are stored as float.hex() strings so the fixtures are bit-exact.
-Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py [swift]
 """
 from __future__ import annotations
 
 import ctypes as C
 import json
 import os
+import re
 import subprocess
 import sys
 from pathlib import Path
@@ -49,8 +55,48 @@ CASES = [
 ]
 
 
+def _numbers(text):
+    return [float(x) for x in re.findall(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?", text)]
+
+
+def _block(src, start_pat, end_pat="};"):
+    i = re.search(start_pat, src).end()
+    j = src.index(end_pat, i)
+    return src[i:j]
+
+
+def swift_golden():
+    """The SWIFT known answers of src/UnitTest.cpp, parsed from its text."""
+    src = (REF / "UnitTest.cpp").read_text()
+    expiries = _numbers(_block(src, r"std::vector<double>\s+expiries\s*=\s*\{"))
+    strikes_txt = _block(src, r"std::vector<std::vector<double>>\s+strikes\s*=\s*\{", "};")
+    strikes = [_numbers(row) for row in re.findall(r"\{([^{}]*)\}", strikes_txt)]
+    params_txt = _block(src, r"std::vector<swift_parameters>\s+params\s*=\s*\{", "};")
+    swift = [_numbers(row) for row in re.findall(r"\{([^{}]*)\}", params_txt)]
+    p_txt = _block(src, r"double\s+p\[5\]\s*=\s*\{", "};")
+    p5 = [float(x) for x in re.findall(r"([-+]?\d*\.\d+|\d+\.)", re.sub(r"//[^\n]*", "", p_txt))]
+    prices = _numbers(_block(src, r"std::vector<ffloat>\s+prices\s*=\s*\{"))
+    grad = _numbers(_block(src, r"std::vector<ffloat>\s+grad\s*=\s*\{"))
+    index_map = [int(x) for x in _numbers(_block(src, r"std::vector<ffloat>\s+index_map\s*=\s*\{"))]
+    risk_free = float(re.search(r"HDistribution new_distr\(heston_params,expiries_arg\[i\],([0-9.]+)\)", src).group(1))
+    tol_p = float(re.search(r"#define PRICING_TOLERANCE\s+(\S+)", src).group(1))
+    tol_g = float(re.search(r"#define GRADIENT_TOLERANCE\s+(\S+)", src).group(1))
+    assert len(expiries) == 8 and len(strikes) == 8 and len(swift) == 8 and len(p5) == 5
+    assert len(prices) == 40 and len(grad) == 200 and sorted(index_map) == [0, 1, 2, 3, 4]
+    out = {"source": "src/UnitTest.cpp pricing_test / gradient_test", "S": 1.0, "r": risk_free,
+           "params5": p5, "expiries": expiries, "strikes": strikes, "swift_params": swift,
+           "prices": [float(x).hex() for x in prices], "grad": [float(x).hex() for x in grad],
+           "grad_index_map": index_map, "price_tolerance_sum_abs": tol_p, "grad_tolerance_sum_abs": tol_g}
+    (HERE / "swift_golden.json").write_text(json.dumps(out, indent=1))
+
+
 def main():
     if not (REF / "RNG.cpp").exists():
+        print("reference checkout not found; nothing to do", file=sys.stderr)
+        return 1
+    swift_golden()
+    if sys.argv[1:] == ["swift"]:
+        return 0
         print("reference checkout not found; nothing to do", file=sys.stderr)
         return 1
     subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref"], check=True)
