@@ -69,21 +69,20 @@ __global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_
     const uint32_t bd = blockDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint64_t *raw = reinterpret_cast<uint64_t *>(smem_raw);
     float *nrm = reinterpret_cast<float *>(raw + 2 * kRngWords * bd);
-    float *tq_r = nrm + 2 * kRngWords * bd;
-    uint16_t *tq_i = reinterpret_cast<uint16_t *>(tq_r + (bd >> 5) * 64);
+    uint16_t *tq_i = reinterpret_cast<uint16_t *>(nrm + 2 * kRngWords * bd);
     uint8_t *tbl = reinterpret_cast<uint8_t *>(tq_i + (bd >> 5) * 64);
     const uint32_t k = blockIdx.x * bd + tid;
     dev::Ring r{raw + tid, nrm + tid, bd};
-    dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tbl + warp * 32, tq_r + warp * 64, tq_i + warp * 64, lane};
+    dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tbl + warp * 32, tq_i + warp * 64, lane};
     dev::Shishua g;
     dev::RngLane c;
-    dev::rng_start(g, c, r, ws, seed + k);
+    dev::rng_start<true>(g, c, r, ws, seed + k);
     for (uint32_t i = 0; i < n; i += 2) {
-        dev::rng_topup(g, c, r, ws);   // same cadence as one QE step (two draws)
+        dev::rng_topup<true>(g, c, r, ws);   // same cadence as one QE step (two draws)
         for (uint32_t h = i; h < i + 2 && h < n; ++h) {
             double v;
             if (kinds[h]) v = dev::uniform_f64(dev::rng_next_u(g, c, r));
-            else v = (double)dev::rng_next_g(g, c, r);
+            else v = (double)dev::rng_next_g<true>(g, c, r);
             if (k < n_streams) out[(size_t)k * n + h] = v;
         }
     }
@@ -91,7 +90,10 @@ __global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_
 
 __global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = (double)dev::as241_word(words[i]);
+    if (i < n) {   // both input stages; a disagreement shows as NaN
+        const float a = dev::as241_word<false>(words[i]), b = dev::as241_word<true>(words[i]);
+        out[i] = __float_as_uint(a) == __float_as_uint(b) ? (double)a : __longlong_as_double(0x7ff8000000000badll);
+    }
 }
 
 cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st) {
@@ -102,7 +104,7 @@ cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words
 cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
                              cudaStream_t st) {
     const uint32_t bd = 64;
-    const size_t smem = (size_t)2 * kRngWords * bd * (sizeof(uint64_t) + sizeof(float)) + (bd / 32) * (64 * 4 + 64 * 2 + 32);
+    const size_t smem = (size_t)2 * kRngWords * bd * (sizeof(uint64_t) + sizeof(float)) + (bd / 32) * kWarpScratchBytes;
     dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, n_streams, kinds, n, out);
     return cudaGetLastError();
 }

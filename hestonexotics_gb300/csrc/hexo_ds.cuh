@@ -70,21 +70,46 @@ __device__ __forceinline__ F2 sqr(F2 x) {
     e = __fmaf_rn(__fadd_rn(x.h, x.h), x.l, e);
     return fast_two_sum(p, e);
 }
-// x / y, y != 0: one float quotient, its remainder in double-single, one correction.
-__device__ __forceinline__ F2 div(F2 x, F2 y) {
-    const float r = __frcp_rn(y.h);
-    const float q1 = __fmul_rn(x.h, r);
-    const F2 rem = add(x, neg(mul_f(y, q1)));
-    const float q2 = __fmul_rn(rem.h, r);
-    return fast_two_sum(q1, q2);
+// Approximate MUFU reciprocal and reciprocal square root.  Each is a fixed
+// function of its input, so results stay reproducible; the Newton-style
+// corrections below bring the double-single results to full precision.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
-// sqrt(x), x > 0: a float root and one Newton correction.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// x * c + d
+__device__ __forceinline__ F2 fma(F2 x, F2 c, F2 d) {
+    const float p = __fmul_rn(x.h, c.h);
+    float e = __fmaf_rn(x.h, c.h, -p);
+    e = __fmaf_rn(x.h, c.l, e);
+    e = __fmaf_rn(x.l, c.h, e);
+    const F2 s = two_sum(p, d.h);
+    return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(e, d.l)));
+}
+// x / y, y > 0 normal: a float quotient q1 from the approximate reciprocal,
+// the remainder x - q1 y (its leading part exact by FMA), one correction.
+__device__ __forceinline__ F2 div(F2 x, F2 y) {
+    const float r = rcp_approx(y.h);
+    const float q1 = __fmul_rn(x.h, r);
+    float e = __fmaf_rn(-q1, y.h, x.h);
+    e = __fadd_rn(e, x.l);
+    e = __fmaf_rn(-q1, y.l, e);
+    return fast_two_sum(q1, __fmul_rn(e, r));
+}
+// sqrt(x), x > 0 normal: a float root from the approximate reciprocal square
+// root and one Newton correction with the exact residual x - s^2.
 __device__ __forceinline__ F2 sqrt(F2 x) {
-    const float rs = rsqrtf(x.h);
+    const float rs = rsqrt_approx(x.h);
     const float s = __fmul_rn(x.h, rs);
-    const F2 sq = sqr(F2{s, 0.0f});
-    const F2 d = add(x, neg(sq));
-    return fast_two_sum(s, __fmul_rn(__fmul_rn(d.h, 0.5f), rs));
+    float e = __fmaf_rn(-s, s, x.h);
+    e = __fadd_rn(e, x.l);
+    return fast_two_sum(s, __fmul_rn(e, __fmul_rn(0.5f, rs)));
 }
 // x < y
 __device__ __forceinline__ bool less(F2 x, F2 y) { return x.h < y.h || (x.h == y.h && x.l < y.l); }

@@ -55,10 +55,10 @@ __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, 
     const bool quad = sp2 < __dmul_rn(1.5, mm);                              // Psi < PSI_C, tpp:61,63
     float z1f = 0.0f;                                                        // draw order, tpp:67,72,80
     uint64_t uw = 0;
-    if (quad) z1f = dev::rng_next_g(g, c, r);
+    if (quad) z1f = dev::rng_next_g<false>(g, c, r);
     else uw = dev::rng_next_u(g, c, r);
     const double z1 = (double)z1f;
-    const double z2 = (double)dev::rng_next_g(g, c, r);
+    const double z2 = (double)dev::rng_next_g<false>(g, c, r);
     double vn;
     if (quad) {                                                              // tpp:64-68
         const double inv = __ddiv_rn(__dmul_rn(2.0, mm), sp2);               // 2/Psi
@@ -91,8 +91,8 @@ __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, 
 __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
                                         const dev::Ring &r, float S0, float rr) {
     const ds::F2 v = pv.vd;
-    const ds::F2 m = ds::add(ds::mul(v, ds::F2{sg.ds_disc[0], sg.ds_disc[1]}), ds::F2{sg.ds_m0[0], sg.ds_m0[1]});
-    const ds::F2 sp2 = ds::add(ds::mul(v, ds::F2{sg.ds_cA[0], sg.ds_cA[1]}), ds::F2{sg.ds_cB[0], sg.ds_cB[1]});
+    const ds::F2 m = ds::fma(v, ds::F2{sg.ds_disc[0], sg.ds_disc[1]}, ds::F2{sg.ds_m0[0], sg.ds_m0[1]});
+    const ds::F2 sp2 = ds::fma(v, ds::F2{sg.ds_cA[0], sg.ds_cA[1]}, ds::F2{sg.ds_cB[0], sg.ds_cB[1]});
     const ds::F2 mm = ds::sqr(m);
     // Psi < PSI_C; the float comparison decides unless it is within 2^-20 of the threshold
     const float t15 = __fmul_rn(1.5f, mm.h);
@@ -100,9 +100,9 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
                                                                                  : ds::less(sp2, ds::mul_f(mm, 1.5f));
     float z1 = 0.0f;
     uint64_t uw = 0;
-    if (quad) z1 = dev::rng_next_g(g, c, r);
+    if (quad) z1 = dev::rng_next_g<true>(g, c, r);
     else uw = dev::rng_next_u(g, c, r);
-    const float z2 = dev::rng_next_g(g, c, r);
+    const float z2 = dev::rng_next_g<true>(g, c, r);
     ds::F2 vn;
     if (quad) {
         const ds::F2 inv = ds::div(ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)}, sp2);   // 2/Psi
@@ -117,10 +117,9 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
         const float Psi = __fdividef(sp2.h, mm.h);
         const float pp1 = __fadd_rn(Psi, 1.0f);
         const float p = __fdividef(__fsub_rn(Psi, 1.0f), pp1);
-        bool ovf;
-        const uint64_t W = dev::rn53(uw, &ovf);                    // U = W 2^-64, 1 - U = (2^64 - W) 2^-64
-        const float U = ovf ? 1.0f : (W == 0 ? 0.0f : dev::u64_to_float_2m64(W));
-        const float omU = ovf ? 0.0f : (W == 0 ? 1.0f : dev::u64_to_float_2m64(0ull - W));
+        const double Ud = dev::uniform_f64(uw);                    // FP64 pipe: idle in this form
+        const float U = __double2float_rn(Ud);
+        const float omU = __double2float_rn(__dsub_rn(1.0, Ud));
         // v = log((1-p)/(1-U)) / beta with 1-p = 2/(Psi+1), 1/beta = m (Psi+1) / 2; never below 0
         const float lr = __logf(__fdividef(__fdividef(2.0f, pp1), omU));
         vn = ds::F2{p < U ? fmaxf(0.0f, __fmul_rn(__fmul_rn(__fmul_rn(0.5f, m.h), pp1), lr)) : 0.0f, 0.0f};
@@ -159,11 +158,10 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     // shared memory: raw words, normals, per-warp conversion scratch
     uint64_t *raw_all = reinterpret_cast<uint64_t *>(smem_raw);
     float *nrm_all = reinterpret_cast<float *>(raw_all + (size_t)PPT * 2 * kRngWords * bd);
-    float *tq_r_all = nrm_all + (size_t)PPT * 2 * kRngWords * bd;
-    uint16_t *tq_i_all = reinterpret_cast<uint16_t *>(tq_r_all + (bd >> 5) * 64);
+    uint16_t *tq_i_all = reinterpret_cast<uint16_t *>(nrm_all + (size_t)PPT * 2 * kRngWords * bd);
     uint8_t *tbl_all = reinterpret_cast<uint8_t *>(tq_i_all + (bd >> 5) * 64);
     unsigned long long *win = reinterpret_cast<unsigned long long *>(
-        smem_raw + ((size_t)PPT * 2 * kRngWords * bd * 12 + (size_t)(bd >> 5) * 416 + 15) / 16 * 16);
+        smem_raw + ((size_t)PPT * 2 * kRngWords * bd * 12 + (size_t)(bd >> 5) * kWarpScratchBytes + 15) / 16 * 16);
 
     dev::Ring ring[PPT];
     dev::WarpScratch ws[PPT];
@@ -175,7 +173,6 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         ws[p].raw0 = ring[p].raw - lane;
         ws[p].nrm0 = ring[p].nrm - lane;
         ws[p].tbl = tbl_all + warp * 32;
-        ws[p].tq_r = tq_r_all + warp * 64;
         ws[p].tq_i = tq_i_all + warp * 64;
         ws[p].lane = lane;
     }
@@ -218,7 +215,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         for (int p = 0; p < PPT; ++p) {
             kpath[p] = td.path_begin + (uint64_t)p * bd + tid;
             active[p] = kpath[p] < S.n_paths;
-            dev::rng_start(g[p], c[p], ring[p], ws[p], S.seed + (uint32_t)kpath[p]);
+            dev::rng_start<kF32>(g[p], c[p], ring[p], ws[p], S.seed + (uint32_t)kpath[p]);
             pv[p].vd = ds::F2{S.ds_v0[0], S.ds_v0[1]};
             pv[p].lx = kF32 ? (R)(-(float)S.f_r * S.f_v0) : (R)S.logS0;   // FP32: log X - log S0 - (rho/sigma) v
             pv[p].v = kF32 ? (R)S.f_v0 : (R)S.v0;
@@ -235,7 +232,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             for (uint32_t st = 1; st < sg.n_steps; ++st) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
-                    dev::rng_topup(g[p], c[p], ring[p], ws[p]);
+                    dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
                     if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf);
                     else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
                     pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
@@ -244,7 +241,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             // the pricing step
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
-                dev::rng_topup(g[p], c[p], ring[p], ws[p]);
+                dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
                 if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf);
                 else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
             }
