@@ -70,10 +70,9 @@ __global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_
     uint64_t *raw = reinterpret_cast<uint64_t *>(smem_raw);
     float *nrm = reinterpret_cast<float *>(raw + 2 * kRngWords * bd);
     uint16_t *tq_i = reinterpret_cast<uint16_t *>(nrm + 2 * kRngWords * bd);
-    uint8_t *tbl = reinterpret_cast<uint8_t *>(tq_i + (bd >> 5) * 64);
     const uint32_t k = blockIdx.x * bd + tid;
     dev::Ring r{raw + tid, nrm + tid, bd};
-    dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tbl + warp * 32, tq_i + warp * 64, lane};
+    dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tq_i + warp * kConvQueue, lane};
     dev::Shishua g;
     dev::RngLane c;
     dev::rng_start<true>(g, c, r, ws, seed + k);

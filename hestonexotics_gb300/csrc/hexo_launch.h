@@ -8,9 +8,9 @@
 namespace hexo {
 
 // Dynamic shared memory of the path kernel: per path two raw slots (16 x u64)
-// and two normal slots (16 x f32); per warp the conversion tables
-// (kWarpScratchBytes: 64 queued items, 32 lane entries); the 64-option staging
-// window of the payoff sums (16-byte aligned).
+// and two normal slots (16 x f32); per warp the conversion queue
+// (kWarpScratchBytes); the 64-option staging window of the payoff sums
+// (16-byte aligned).
 inline size_t paths_smem_bytes(uint32_t block, uint32_t ppt) {
     const size_t rings = (size_t)ppt * 2 * kRngWords * block * (sizeof(uint64_t) + sizeof(float)) +
                          (size_t)(block / 32) * kWarpScratchBytes;

@@ -159,7 +159,6 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     uint64_t *raw_all = reinterpret_cast<uint64_t *>(smem_raw);
     float *nrm_all = reinterpret_cast<float *>(raw_all + (size_t)PPT * 2 * kRngWords * bd);
     uint16_t *tq_i_all = reinterpret_cast<uint16_t *>(nrm_all + (size_t)PPT * 2 * kRngWords * bd);
-    uint8_t *tbl_all = reinterpret_cast<uint8_t *>(tq_i_all + (bd >> 5) * 64);
     unsigned long long *win = reinterpret_cast<unsigned long long *>(
         smem_raw + ((size_t)PPT * 2 * kRngWords * bd * 12 + (size_t)(bd >> 5) * kWarpScratchBytes + 15) / 16 * 16);
 
@@ -172,8 +171,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         ring[p].stride = bd;
         ws[p].raw0 = ring[p].raw - lane;
         ws[p].nrm0 = ring[p].nrm - lane;
-        ws[p].tbl = tbl_all + warp * 32;
-        ws[p].tq_i = tq_i_all + warp * 64;
+        ws[p].tq_i = tq_i_all + warp * kConvQueue;
         ws[p].lane = lane;
     }
     __shared__ uint32_t s_tile;

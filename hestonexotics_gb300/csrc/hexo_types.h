@@ -18,7 +18,8 @@ constexpr int kLimbs = 6;            // 3 x 25-bit limbs of sum(pay*2^40), 3 of 
 constexpr int kLimbBits = 25;        // a warp adds up to 128 limb values in 32 bits
 constexpr uint32_t kLimbMask = (1u << kLimbBits) - 1u;
 constexpr int kRngWords = 16;        // words per RNG buffer (one SHISHUA block)
-constexpr uint32_t kWarpScratchBytes = 64 * 2 + 32;   // per warp: queued conversion items, lane table
+constexpr uint32_t kConvQueue = 96;                    // per warp: queued conversion items
+constexpr uint32_t kWarpScratchBytes = kConvQueue * 2; // per warp: the queue
 constexpr int kRingSlots = 3;        // per path: normal buffer, uniform buffer, one look-ahead block
 
 struct SegDesc {
