@@ -56,6 +56,13 @@ WORKLOAD = "uneven_batch_64sets_fp32_graph"
 # count once each (6 per step).  Total 102.
 ALG_FP32_OPS_PER_PATH_STEP = 102.0
 
+# DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
+# Nsight Compute capture of this workload at 1/16 of its paths (130.2 MB +
+# 88.9 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
+# traffic is the CTA-private sum slots a launch touches plus the descriptors;
+# it does not grow with the path count, so it is reported unscaled.
+PATHS_KERNEL_DRAM_BYTES = 130.2e6 + 88.9e6
+
 
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
@@ -318,14 +325,6 @@ def run_engine(args, rank, world, local):
         kms = statistics.mean(kernel_ms)
         achieved = ALG_FP32_OPS_PER_PATH_STEP * nominal / (kms * 1e-3) / 1e9
         peak = peaks["fp32_fma"] / 1e9
-        profile_traffic = None
-        ptxt = ROOT / "profiles" / "paths_kernel_fp32_traffic.json"
-        if ptxt.exists():
-            try:
-                d = json.loads(ptxt.read_text())
-                profile_traffic = d["dram_bytes_per_path_step"] * nominal
-            except (ValueError, KeyError):
-                profile_traffic = None
         serving = None
         if args.serve_rates:
             rates = [float(x) for x in args.serve_rates.split(",") if x]
@@ -354,7 +353,9 @@ def run_engine(args, rank, world, local):
                            "fp32_within_1se_frac": in_se / max(1, n_opts)},
             "roofline": {"bound": "compute: FP32 pipe (no tensor-core or HBM bound on this path)",
                          "achieved": achieved, "peak": peak, "unit": "Gop/s (FP32-pipe lane ops)",
-                         "frac": achieved / peak, "traffic": profile_traffic,
+                         "frac": achieved / peak, "traffic": PATHS_KERNEL_DRAM_BYTES,
+                         "traffic_note": "DRAM bytes per launch from ncu at 1/16 of the paths; sum slots and "
+                                         "descriptors, independent of the path count",
                          "peak_source": "FP32-FMA lane rate measured in this run by hexo_debug_pipe_peaks",
                          "alg_ops_per_path_step": ALG_FP32_OPS_PER_PATH_STEP, "kernel_ms": kms,
                          "pipe_peaks_lane_ops_per_s": peaks},
