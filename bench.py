@@ -24,6 +24,7 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              host cores) on a bounded sample of the same workload
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+  python bench.py --precision-sweep | --autotune [--path-scale S]   (reports, not the benchmark)
 """
 from __future__ import annotations
 
@@ -231,6 +232,38 @@ def run_serving(eng, rates, duration_s, fp64_rates):
     return out
 
 
+# ------------------------------------------------------ precision sweep
+
+def run_precision_sweep(eng, counts):
+    """The single-chain batch (8 maturities x 50 strikes x Asian/European,
+    seed 1) and the Feller-violating set, FP32 form against the FP64 form on
+    the same streams (the FP64 form matches the oracle to 1e-10), at each
+    path count: worst relative error over prices above 1e-3 S0, worst
+    |error| / standard error, and the median standard error / price."""
+    from hestonexotics_gb300 import FP32, FP64
+    from hestonexotics_gb300 import workloads as W
+    out = []
+    for name, make in (("single_chain_seed1", W.single_chain), ("feller_violating", W.feller_violating)):
+        for n in counts:
+            rq, cfg64 = make(n_paths=n, precision=FP64)
+            _, cfg32 = make(n_paths=n, precision=FP32)
+            t0 = time.perf_counter()
+            p64, se64 = eng.price(rq.params, rq.S0, rq.options, cfg64)
+            t64 = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            p32, se32 = eng.price(rq.params, rq.S0, rq.options, cfg32)
+            t32 = time.perf_counter() - t0
+            big = p64 > 1e-3 * rq.S0
+            rel = np.abs(p32 - p64)[big] / p64[big]
+            z = np.abs(p32 - p64) / np.maximum(se64, 1e-300)
+            out.append({"set": name, "paths": n, "options": len(p64), "max_rel_err": float(rel.max()),
+                        "median_rel_err": float(np.median(rel)), "max_err_over_se": float(z.max()),
+                        "within_1se_frac": float(np.mean(z <= 1.0)),
+                        "median_se_over_price": float(np.median(se64[big] / p64[big])),
+                        "fp64_s": t64, "fp32_s": t32})
+    return out
+
+
 # -------------------------------------------------------------- engine arm
 
 def run_engine(args, rank, world, local):
@@ -239,6 +272,16 @@ def run_engine(args, rank, world, local):
     from hestonexotics_gb300 import workloads as W
 
     torch.cuda.set_device(local)
+    if args.precision_sweep or args.autotune:
+        eng = Engine(local)
+        out = {"metric": METRIC, "unit": UNIT}
+        if args.precision_sweep:
+            out["precision_sweep"] = run_precision_sweep(eng, [1 << k for k in (16, 18, 20, 22, 24)])
+        if args.autotune:
+            reqs, cfg = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale)
+            out["autotune"] = {"workload": f"{WORKLOAD}_paths_x{args.path_scale:g}", **eng.autotune(reqs, cfg)}
+        eng.close()
+        return out if rank == 0 else None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -399,6 +442,10 @@ def main():
     ap.add_argument("--serve-rates", default="50,200,500,2000", help="request rates of the serving leg ('' = skip)")
     ap.add_argument("--serve-fp64-rates", default="50,200", help="rates also priced one request per FP64 launch")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="instead of the benchmark: FP32 vs FP64 errors on the single chain at 2^16..2^24 paths")
+    ap.add_argument("--autotune", action="store_true",
+                    help="instead of the benchmark: the launch-shape sweep on the uneven batch (use --path-scale)")
     ap.add_argument("--path-scale", type=float, default=1.0,
                     help="scales every path count of the batch (1.0 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()

@@ -5,6 +5,7 @@ include/hexo_mc.h); this package is its Python face:
 
   engine      Engine / Params / Options / Config / Server: typed wrapper of the C ABI
   shard       path-range shards merged exactly across ranks (torch.distributed)
+  paramsdb    the reference's HParams.db parameter store as a request source
   workloads   seeded synthetic workloads with the configurations' shapes
   build       in-tree build of libhexo_mc.so
 """

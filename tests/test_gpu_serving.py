@@ -90,3 +90,19 @@ def test_invalid_request_and_unknown_ticket(engine):
         good = srv.wait(srv.submit(reqs[0]))
     want = engine.price_batch([reqs[0]], cfg)[0]
     assert np.array_equal(good[0], want[0])
+
+
+def test_requests_from_paramsdb(engine, tmp_path):
+    # the serving loop fed by the reference's parameter database (HParams.db)
+    from hestonexotics_gb300.paramsdb import ParamsDB
+    reqs, cfg = small_requests(n=3)
+    with ParamsDB(tmp_path / "HParams.db") as db:
+        for k, rq in enumerate(reqs):
+            db.insertupdate(rq.params, f"U{k}")
+        # the table holds the five Heston parameters; the rate comes with the request
+        from_db = [db.request(f"U{k}", rq.S0, rq.options, seed=rq.seed, r=rq.params.r) for k, rq in enumerate(reqs)]
+    with engine.server(cfg) as srv:
+        got = [srv.wait(srv.submit(rq)) for rq in from_db]
+    for rq, (p, s) in zip(reqs, got):
+        want = engine.price_batch([rq], cfg)[0]
+        assert np.array_equal(p, want[0]) and np.array_equal(s, want[1])
