@@ -98,6 +98,24 @@ class hexo_server_stats(C.Structure):
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double)]
 
 
+class hexo_swift_params(C.Structure):
+    _fields_ = [("m", C.c_uint32), ("exp2_m", C.c_uint32), ("sqrt_exp2_m", C.c_double), ("lower", C.c_double),
+                ("upper", C.c_double), ("k1", C.c_int32), ("k2", C.c_int32), ("J", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class hexo_swift_chain(C.Structure):
+    _fields_ = [("tau", C.c_double), ("strikes", C.POINTER(C.c_double)), ("n", C.c_uint32),
+                ("reserved", C.c_uint32), ("params", C.POINTER(hexo_swift_params)),
+                ("trunc_precision", C.c_double), ("price_out", C.POINTER(C.c_double)),
+                ("grad_out", C.POINTER(C.c_double))]
+
+
+class hexo_swift_request(C.Structure):
+    _fields_ = [("params", hexo_params), ("S", C.c_double), ("chains", C.POINTER(hexo_swift_chain)),
+                ("n_chains", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _U64 = C.POINTER(C.c_uint64)
@@ -126,6 +144,9 @@ PROTOTYPES = {
     "hexo_server_wait": (C.c_int, [_P, C.c_uint64, C.c_uint32]),
     "hexo_server_stats_get": (C.c_int, [_P, C.POINTER(hexo_server_stats)]),
     "hexo_server_destroy": (C.c_int, [_P]),
+    "hexo_swift_params_dynamic": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_double, C.POINTER(hexo_swift_params)]),
+    "hexo_swift_price": (C.c_int, [_P, C.POINTER(hexo_swift_request), C.c_uint32]),
     "hexo_price_partial": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
     "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.POINTER(hexo_option), C.c_uint32,

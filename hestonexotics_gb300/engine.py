@@ -295,6 +295,50 @@ class Engine:
     def server(self, cfg: Config, **kw) -> Server:
         return Server(self, cfg, **kw)
 
+    def swift(self, params: Params, S: float, chains, grad: bool = False, swift_params=None,
+              trunc_precision: float = 0.0):
+        """SWIFT European call prices (and gradients in v0, theta, rho, kappa,
+        sigma) for chains [(tau, strikes), ...]; swift_params: per chain a
+        dict / 8-sequence of the reference's SwiftParameters, or None for the
+        reference's dynamic choice.  Returns [price] or [(price, grad[n, 5])]."""
+        return self.swift_batch([(params, S, chains)], grad, None if swift_params is None else [swift_params],
+                                trunc_precision)[0]
+
+    def swift_batch(self, requests, grad: bool = False, swift_params=None, trunc_precision: float = 0.0):
+        """requests: [(Params, S, [(tau, strikes), ...]), ...], priced in one call."""
+        reqs = (L.hexo_swift_request * len(requests))()
+        keep, outs = [], []
+        for q, (params, S, chains) in enumerate(requests):
+            arr = (L.hexo_swift_chain * max(1, len(chains)))()
+            res = []
+            for c, (tau, K) in enumerate(chains):
+                K = np.ascontiguousarray(K, dtype=np.float64)
+                price = np.zeros(len(K))
+                g = np.zeros((len(K), 5)) if grad else None
+                arr[c].tau = float(tau)
+                arr[c].strikes = _dp(K)
+                arr[c].n = len(K)
+                sp = swift_params[q][c] if swift_params is not None and swift_params[q] is not None else None
+                if sp is not None:
+                    v = list(sp.values()) if isinstance(sp, dict) else list(sp)
+                    spc = L.hexo_swift_params(int(v[0]), int(v[1]), float(v[2]), float(v[3]), float(v[4]),
+                                              int(v[5]), int(v[6]), int(v[7]), 0)
+                    keep.append(spc)
+                    arr[c].params = C.pointer(spc)
+                arr[c].trunc_precision = trunc_precision
+                arr[c].price_out = _dp(price)
+                arr[c].grad_out = _dp(g) if grad else None
+                keep += [K, price, g]
+                res.append((price, g) if grad else price)
+            keep.append(arr)
+            reqs[q].params = params.c()
+            reqs[q].S = float(S)
+            reqs[q].chains = C.cast(arr, C.POINTER(L.hexo_swift_chain))
+            reqs[q].n_chains = len(chains)
+            outs.append(res)
+        self._check(self._lib.hexo_swift_price(self._ctx, reqs, len(requests)))
+        return outs
+
     def partial(self, params: Params, S0: float, options: Options, cfg: Config, path_lo: int, path_hi: int):
         n = len(options)
         limbs = np.zeros(n * L.HEXO_LIMBS, dtype=np.uint64)
@@ -353,6 +397,17 @@ class Engine:
                                                      C.byref(c), path_lo, path_hi, _dp(a), _dp(e), C.byref(nm)))
         m = nm.value
         return a[: n * m].reshape(n, m), e[: n * m].reshape(n, m)
+
+
+def swift_params_dynamic(params: Params, tau: float, S: float, K_min: float, K_max: float,
+                         trunc_precision: float = 1e-7) -> dict:
+    """Host-only: the reference's dynamic SWIFT parameters for one expiry (SWIFT.cpp:21-35)."""
+    out = L.hexo_swift_params()
+    p = params.c()
+    st = L.load().hexo_swift_params_dynamic(C.byref(p), tau, S, K_min, K_max, trunc_precision, C.byref(out))
+    if st != L.HEXO_OK:
+        raise L.HexoError(st, "hexo_swift_params_dynamic")
+    return {k: getattr(out, k) for k in ("m", "exp2_m", "sqrt_exp2_m", "lower", "upper", "k1", "k2", "J")}
 
 
 def finalize_limbs(params: Params, options: Options, cfg: Config, limbs: np.ndarray):

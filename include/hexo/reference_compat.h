@@ -54,6 +54,10 @@ typedef struct OptionsChain {
     std::vector<option> options;
     unsigned int days_to_expiry;
     ffloat time_to_expiry, max_strike, min_strike;
+    OptionsChain(unsigned int days_until, ffloat time_until)
+        : days_to_expiry(days_until), time_to_expiry(time_until), max_strike(-1.7976931348623157e308),
+          min_strike(1.7976931348623157e308) {}
+    OptionsChain(OptionsChain &&) = default;
 } options_chain;
 class AAsianCallNonAdaptive;
 class EuropeanCallNonAdaptive;

@@ -225,6 +225,53 @@ hexo_status hexo_server_stats_get(hexo_server *s, hexo_server_stats *out);
  * from other threads get HEXO_ERR_SHUTDOWN. */
 hexo_status hexo_server_destroy(hexo_server *s);
 
+/* ------------------------------------------------------ SWIFT Europeans */
+
+/* European calls by the SWIFT wavelet method with their gradients in
+ * (v0, theta, rho, kappa, sigma): the reference's SWIFT::price_opts and
+ * price_opts_grad (src/SWIFT.cpp:87-118, src/inc/SWIFT.h:150-164) with the
+ * characteristic function of src/HDistribution.cpp, batched on the GPU in
+ * FP64.  It is the reference's calibration objective and the check for the
+ * Monte Carlo European prices. */
+
+/* The reference's SwiftParameters (src/inc/SWIFT.h:27-76), same fields. */
+typedef struct hexo_swift_params {
+    uint32_t m, exp2_m;       /* wavelet scale m and 2^m */
+    double sqrt_exp2_m;
+    double lower, upper;      /* integration range of the log-price */
+    int32_t k1, k2;           /* sum range */
+    uint32_t J, reserved;     /* frequencies (a power of two, at most 2048); reserved = 0 */
+} hexo_swift_params;
+
+/* Host-only: the reference's dynamic choice of the parameters for one expiry
+ * (SwiftParameters(distr, S, chain), src/SWIFT.cpp:21-35): the smallest m
+ * whose truncation error is below trunc_precision, plus one (the reference's
+ * loop), and the range from the first, second and fourth cumulants.
+ * trunc_precision: 1e-7 in the reference's release build (FASTMATH), 1e-10
+ * otherwise (SWIFT.cpp:12-16).  Uses p->r as the risk-free rate. */
+hexo_status hexo_swift_params_dynamic(const hexo_params *p, double tau, double S, double K_min, double K_max,
+                                      double trunc_precision, hexo_swift_params *out);
+
+typedef struct hexo_swift_chain {
+    double tau;                        /* years to expiry */
+    const double *strikes;             /* n strikes */
+    uint32_t n, reserved;
+    const hexo_swift_params *params;   /* NULL: chosen as hexo_swift_params_dynamic does */
+    double trunc_precision;            /* for params == NULL; 0 = 1e-7 */
+    double *price_out;                 /* n discounted call prices */
+    double *grad_out;                  /* n x 5 (v0, theta, rho, kappa, sigma), row per option; may be NULL */
+} hexo_swift_chain;
+
+typedef struct hexo_swift_request {
+    hexo_params params;                /* r is the risk-free rate; q must be 0 */
+    double S;
+    const hexo_swift_chain *chains;
+    uint32_t n_chains, reserved;
+} hexo_swift_request;
+
+/* Prices every chain of every request in one sequence of launches; blocks. */
+hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint32_t n_reqs);
+
 /* --------------------------------------------------------------- shards */
 
 /* Exact partial sums over paths [path_lo, path_hi) of one request: for each

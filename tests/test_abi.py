@@ -42,7 +42,8 @@ def test_every_declared_function_is_exported(lib):
 
 def test_struct_layouts_match_header(tmp_path):
     structs = ["hexo_params", "hexo_option", "hexo_mc_cfg", "hexo_ctx_opts", "hexo_request", "hexo_batch_info",
-               "hexo_plan_stats", "hexo_tune_result", "hexo_tune_entry", "hexo_server_opts", "hexo_server_stats"]
+               "hexo_plan_stats", "hexo_tune_result", "hexo_tune_entry", "hexo_server_opts", "hexo_server_stats",
+               "hexo_swift_params", "hexo_swift_chain", "hexo_swift_request"]
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include "hexo_mc.h"\nint main(void){\n' +
                    "".join(f'printf("%zu\\n", sizeof({s}));\n' for s in structs) + "return 0;}\n")

@@ -1,0 +1,64 @@
+"""SWIFT European pricer of the library (hexo_swift_*).
+
+CPU: the dynamic wavelet parameters (host-only) equal the oracle's
+restatement of SwiftParameters (src/SWIFT.cpp:21-35) exactly.
+GPU: prices and gradients against the reference's known answers
+(src/UnitTest.cpp pricing_test / gradient_test, sum of absolute differences
+below 1e-9 as there), and against the oracle's restatement on other
+parameter sets to 1e-10 absolute (S = 100: relative to the strike scale).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, unhex
+from hestonexotics_gb300 import engine as E
+
+
+def _golden():
+    g = golden("swift_golden.json")
+    p = E.Params(*g["params5"], r=g["r"])
+    chains = [(T, np.array(K)) for T, K in zip(g["expiries"], g["strikes"])]
+    return g, p, chains
+
+
+def test_dynamic_params_equal_oracle(oracle):
+    g, p, chains = _golden()
+    for prec in (1e-7, 1e-10):
+        for T, K in chains:
+            got = E.swift_params_dynamic(p, T, g["S"], K.min(), K.max(), prec)
+            want = oracle.swift_params(g["params5"], T, g["r"], g["S"], K.min(), K.max(), trunc_precision=prec)
+            assert [got["m"], got["exp2_m"], got["k1"], got["k2"], got["J"]] == [int(want[0]), int(want[1]),
+                                                                               int(want[5]), int(want[6]), int(want[7])]
+            np.testing.assert_allclose([got["sqrt_exp2_m"], got["lower"], got["upper"]], want[[2, 3, 4]], rtol=1e-13)
+
+
+@pytest.mark.gpu
+def test_gpu_golden_prices_and_gradients(engine):
+    g, p, chains = _golden()
+    out = engine.swift(p, g["S"], chains, grad=True, swift_params=g["swift_params"])
+    price = np.concatenate([o[0] for o in out])
+    grad = np.concatenate([o[1] for o in out])
+    assert np.sum(np.abs(price - unhex(g["prices"]))) < g["price_tolerance_sum_abs"]
+    want = unhex(g["grad"]).reshape(40, 5)
+    imap = g["grad_index_map"]
+    diff = sum(abs(want[i, imap[j]] - grad[i, j]) for i in range(40) for j in range(5))
+    assert diff < g["grad_tolerance_sum_abs"]
+
+
+@pytest.mark.gpu
+def test_gpu_matches_oracle_dynamic(engine, oracle):
+    rng = np.random.default_rng(4)
+    reqs, wants = [], []
+    for _ in range(6):
+        p5 = [rng.uniform(0.01, 0.09), rng.uniform(0.01, 0.09), rng.uniform(-0.9, -0.1), rng.uniform(0.5, 5.0),
+              rng.uniform(0.1, 1.0)]
+        r = rng.uniform(0.0, 0.05)
+        chains = [(T, np.geomspace(60.0, 160.0, 25)) for T in (1 / 12, 0.5, 2.0)]
+        reqs.append((E.Params(*p5, r=r), 100.0, chains))
+        wants.append([oracle.swift_price(p5, T, r, 100.0, K, oracle.swift_params(p5, T, r, 100.0, K.min(), K.max()),
+                                         grad=True) for T, K in chains])
+    outs = engine.swift_batch(reqs, grad=True)
+    for out, want in zip(outs, wants):
+        for (gp, gg), (wp, wg) in zip(out, want):
+            np.testing.assert_allclose(gp, wp, rtol=0, atol=1e-10)
+            np.testing.assert_allclose(gg, wg, rtol=0, atol=1e-8)
