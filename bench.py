@@ -24,7 +24,7 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              host cores) on a bounded sample of the same workload
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
-  python bench.py --precision-sweep | --autotune [--path-scale S]   (reports, not the benchmark)
+  python bench.py --precision-sweep | --swift | --autotune [--path-scale S]   (reports, not the benchmark)
 """
 from __future__ import annotations
 
@@ -264,6 +264,55 @@ def run_precision_sweep(eng, counts):
     return out
 
 
+# ------------------------------------------------------------------ SWIFT
+
+def run_swift_report(eng, n_sets=1024):
+    """SWIFT European prices with gradients: the reference's calibration
+    objective (8 chains x 5 strikes, the unit tests' chains, dynamic
+    wavelet parameters) per evaluation on the GPU and in the oracle's CPU
+    restatement (one thread, direct sums instead of FFTW), and a batch of
+    parameter sets x 8 chains x 50 strikes."""
+    import json as _json
+    from hestonexotics_gb300 import engine as E
+    from hestonexotics_gb300 import workloads as W
+    from oracle import oracle as O
+    g = _json.loads((ROOT / "tests" / "golden" / "swift_golden.json").read_text())
+    chains = [(T, np.array(K)) for T, K in zip(g["expiries"], g["strikes"])]
+    cal = eng.calibration(g["S"], g["r"], chains)
+    p = np.array(g["params5"])
+    for _ in range(3):
+        cal.jacobian(p + 1e-9 * _)
+    ts = []
+    for k in range(50):
+        q = p * (1.0 + 1e-6 * (k + 1))      # a new p each time: no cached evaluation
+        t0 = time.perf_counter()
+        cal.prices(q)
+        cal.jacobian(q)
+        ts.append(time.perf_counter() - t0)
+    gpu_ms = 1e3 * statistics.median(ts)
+    O.build()
+    t0 = time.perf_counter()
+    for T, K in chains:
+        sp = O.swift_params(g["params5"], T, g["r"], g["S"], K.min(), K.max())
+        O.swift_price(g["params5"], T, g["r"], g["S"], K, sp, grad=True)
+    cpu_ms = 1e3 * (time.perf_counter() - t0)
+    rng = np.random.default_rng(5)
+    reqs = []
+    for _ in range(n_sets):
+        prm = W.draw_params(rng)
+        reqs.append((prm, 100.0, [(T, np.geomspace(60.0, 160.0, 50)) for T in W.CHAIN_MATURITIES]))
+    eng.swift_batch(reqs[:8], grad=True)
+    t0 = time.perf_counter()
+    eng.swift_batch(reqs, grad=True)
+    tb = time.perf_counter() - t0
+    n_opts = n_sets * len(W.CHAIN_MATURITIES) * 50
+    return {"calibration_eval": {"chains": 8, "observations": 40, "gpu_ms_prices_and_jacobian": gpu_ms,
+                                 "oracle_cpu_ms_1_thread": cpu_ms,
+                                 "oracle_note": "direct-sum restatement; the reference uses FFTW and Eigen"},
+            "batch": {"sets": n_sets, "chains_per_set": len(W.CHAIN_MATURITIES), "strikes_per_chain": 50,
+                      "seconds": tb, "options_per_s_with_gradients": n_opts / tb}}
+
+
 # -------------------------------------------------------------- engine arm
 
 def run_engine(args, rank, world, local):
@@ -272,11 +321,13 @@ def run_engine(args, rank, world, local):
     from hestonexotics_gb300 import workloads as W
 
     torch.cuda.set_device(local)
-    if args.precision_sweep or args.autotune:
+    if args.precision_sweep or args.autotune or args.swift:
         eng = Engine(local)
         out = {"metric": METRIC, "unit": UNIT}
         if args.precision_sweep:
             out["precision_sweep"] = run_precision_sweep(eng, [1 << k for k in (16, 18, 20, 22, 24)])
+        if args.swift:
+            out["swift"] = run_swift_report(eng)
         if args.autotune:
             reqs, cfg = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale)
             out["autotune"] = {"workload": f"{WORKLOAD}_paths_x{args.path_scale:g}", **eng.autotune(reqs, cfg)}
@@ -444,6 +495,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--precision-sweep", action="store_true",
                     help="instead of the benchmark: FP32 vs FP64 errors on the single chain at 2^16..2^24 paths")
+    ap.add_argument("--swift", action="store_true",
+                    help="instead of the benchmark: SWIFT pricer and calibration-callback timings")
     ap.add_argument("--autotune", action="store_true",
                     help="instead of the benchmark: the launch-shape sweep on the uneven batch (use --path-scale)")
     ap.add_argument("--path-scale", type=float, default=1.0,

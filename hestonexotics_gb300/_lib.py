@@ -147,6 +147,12 @@ PROTOTYPES = {
     "hexo_swift_params_dynamic": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_double, C.POINTER(hexo_swift_params)]),
     "hexo_swift_price": (C.c_int, [_P, C.POINTER(hexo_swift_request), C.c_uint32]),
+    "hexo_calib_create": (C.c_int, [_P, C.c_double, C.c_double, _D, C.POINTER(C.c_uint32), _D, C.c_uint32, C.c_double,
+                                    C.POINTER(_P)]),
+    "hexo_calib_observations": (C.c_uint32, [_P]),
+    "hexo_calib_prices": (C.c_int, [_P, _D, _D]),
+    "hexo_calib_jacobian": (C.c_int, [_P, _D, _D]),
+    "hexo_calib_destroy": (C.c_int, [_P]),
     "hexo_price_partial": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
     "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.POINTER(hexo_option), C.c_uint32,

@@ -484,4 +484,103 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
     return HEXO_OK;
 }
 
+// ------------------------------------------------ calibration callbacks
+
+// The reference's calibration data (adata_s, src/inc/HCalibration.h:13-30):
+// the spot and every chain's expiry and strikes.  prices / jacobian are the
+// objective and Jacobian that its Levenberg-Marquardt call evaluates
+// (get_prices_for_levmar / get_jacobian_for_levmar, HCalibration.cpp:35-57):
+// for a parameter vector p = (v0, vm, rho, kappa, sigma) the wavelet
+// parameters of every chain are chosen for p (update_adata,
+// HCalibration.cpp:11-33), then all chains are priced in one call.  The last
+// p's prices and Jacobian are kept, so the pair of calls levmar makes per
+// step prices once.
+struct hexo_calib {
+    hexo_ctx *ctx = nullptr;
+    double S = 0.0, r = 0.0, trunc = 1e-7;
+    std::vector<double> taus, strikes;
+    std::vector<uint32_t> counts;
+    bool have = false;
+    double last_p[5] = {0, 0, 0, 0, 0};
+    std::vector<double> prices, jac;
+};
+
+namespace {
+hexo_status calib_eval(hexo_calib *c, const double *p) {
+    if (c->have && std::memcmp(p, c->last_p, sizeof c->last_p) == 0) return HEXO_OK;
+    const size_t n = c->strikes.size();
+    c->prices.assign(n, 0.0);
+    c->jac.assign(n * 5, 0.0);
+    std::vector<hexo_swift_chain> chains(c->taus.size());
+    size_t off = 0;
+    for (size_t k = 0; k < chains.size(); ++k) {
+        hexo_swift_chain &ch = chains[k];
+        std::memset(&ch, 0, sizeof ch);
+        ch.tau = c->taus[k];
+        ch.strikes = c->strikes.data() + off;
+        ch.n = c->counts[k];
+        ch.params = nullptr;
+        ch.trunc_precision = c->trunc;
+        ch.price_out = c->prices.data() + off;
+        ch.grad_out = c->jac.data() + off * 5;
+        off += c->counts[k];
+    }
+    hexo_swift_request rq;
+    std::memset(&rq, 0, sizeof rq);
+    rq.params = hexo_params{p[0], p[1], p[2], p[3], p[4], c->r, 0.0};
+    rq.S = c->S;
+    rq.chains = chains.data();
+    rq.n_chains = (uint32_t)chains.size();
+    const hexo_status s = hexo_swift_price(c->ctx, &rq, 1);
+    c->have = s == HEXO_OK;
+    if (c->have) std::memcpy(c->last_p, p, sizeof c->last_p);
+    return s;
+}
+} // namespace
+
+hexo_status hexo_calib_create(hexo_ctx *ctx, double S, double r, const double *taus, const uint32_t *counts,
+                              const double *strikes, uint32_t n_chains, double trunc_precision, hexo_calib **out) {
+    if (!ctx || !out || !taus || !counts || !strikes || n_chains == 0 || !(S > 0.0) || !std::isfinite(r))
+        return HEXO_ERR_INVALID;
+    *out = nullptr;
+    hexo_calib *c = new (std::nothrow) hexo_calib();
+    if (!c) return HEXO_ERR_NOMEM;
+    c->ctx = ctx;
+    c->S = S;
+    c->r = r;
+    c->trunc = trunc_precision > 0.0 ? trunc_precision : 1e-7;
+    size_t n = 0;
+    for (uint32_t k = 0; k < n_chains; ++k) {
+        if (!(taus[k] > 0.0) || counts[k] == 0) { delete c; return HEXO_ERR_INVALID; }
+        c->taus.push_back(taus[k]);
+        c->counts.push_back(counts[k]);
+        n += counts[k];
+    }
+    c->strikes.assign(strikes, strikes + n);
+    *out = c;
+    return HEXO_OK;
+}
+
+uint32_t hexo_calib_observations(const hexo_calib *c) { return c ? (uint32_t)c->strikes.size() : 0u; }
+
+hexo_status hexo_calib_prices(hexo_calib *c, const double *p, double *x) {
+    if (!c || !p || !x) return HEXO_ERR_INVALID;
+    const hexo_status s = calib_eval(c, p);
+    if (s == HEXO_OK) std::memcpy(x, c->prices.data(), c->prices.size() * sizeof(double));
+    return s;
+}
+
+hexo_status hexo_calib_jacobian(hexo_calib *c, const double *p, double *jac) {
+    if (!c || !p || !jac) return HEXO_ERR_INVALID;
+    const hexo_status s = calib_eval(c, p);
+    if (s == HEXO_OK) std::memcpy(jac, c->jac.data(), c->jac.size() * sizeof(double));
+    return s;
+}
+
+hexo_status hexo_calib_destroy(hexo_calib *c) {
+    if (!c) return HEXO_ERR_INVALID;
+    delete c;
+    return HEXO_OK;
+}
+
 } // extern "C"

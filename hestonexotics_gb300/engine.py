@@ -215,6 +215,47 @@ class Server:
             pass
 
 
+class Calibration:
+    """The reference's calibration objective on the GPU (hexo_calib_*):
+    ``prices(p)`` and ``jacobian(p)`` for p = (v0, vm, rho, kappa, sigma), as
+    its Levenberg-Marquardt callbacks compute them."""
+
+    def __init__(self, engine: "Engine", S: float, r: float, chains, trunc_precision: float = 0.0):
+        self.engine = engine
+        self._lib = engine._lib
+        taus = np.ascontiguousarray([t for t, _ in chains], dtype=np.float64)
+        counts = np.ascontiguousarray([len(k) for _, k in chains], dtype=np.uint32)
+        strikes = np.ascontiguousarray(np.concatenate([np.asarray(k, dtype=np.float64) for _, k in chains]))
+        self.n = int(counts.sum())
+        self.handle = C.c_void_p()
+        engine._check(self._lib.hexo_calib_create(engine._ctx, float(S), float(r), _dp(taus),
+                                                  counts.ctypes.data_as(C.POINTER(C.c_uint32)), _dp(strikes),
+                                                  len(counts), float(trunc_precision), C.byref(self.handle)))
+
+    def prices(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        x = np.zeros(self.n)
+        self.engine._check(self._lib.hexo_calib_prices(self.handle, _dp(p), _dp(x)))
+        return x
+
+    def jacobian(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        j = np.zeros((self.n, 5))
+        self.engine._check(self._lib.hexo_calib_jacobian(self.handle, _dp(p), _dp(j)))
+        return j
+
+    def close(self):
+        if self.handle:
+            self._lib.hexo_calib_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Engine:
     def __init__(self, device: int = 0, mem_cap_bytes: int = 0, autotune_cache: str | None = None):
         lib = L.load()
@@ -294,6 +335,9 @@ class Engine:
 
     def server(self, cfg: Config, **kw) -> Server:
         return Server(self, cfg, **kw)
+
+    def calibration(self, S: float, r: float, chains, trunc_precision: float = 0.0) -> Calibration:
+        return Calibration(self, S, r, chains, trunc_precision)
 
     def swift(self, params: Params, S: float, chains, grad: bool = False, swift_params=None,
               trunc_precision: float = 0.0):

@@ -272,6 +272,25 @@ typedef struct hexo_swift_request {
 /* Prices every chain of every request in one sequence of launches; blocks. */
 hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint32_t n_reqs);
 
+/* Calibration callbacks.  The reference calibrates by Levenberg-Marquardt
+ * (levmar's dlevmar_der) over the SWIFT prices of every chain of an
+ * underlying, with the objective and Jacobian callbacks
+ *   void get_prices_for_levmar(double *p, double *x, int m, int n, void *adata);
+ *   void get_jacobian_for_levmar(double *p, double *jac, int m, int n, void *adata);
+ * (src/HCalibration.cpp:35-57).  hexo_calib holds the same data (spot, rate,
+ * each chain's expiry and strikes); hexo_calib_prices / _jacobian compute x
+ * (n observations, chains in order) and jac (n x 5, row per observation,
+ * columns v0, vm, rho, kappa, sigma) for p = {v0, vm, rho, kappa, sigma} on the
+ * GPU, choosing every chain's wavelet parameters for p as update_adata does
+ * (HCalibration.cpp:11-33).  One evaluation serves both calls for the same p. */
+typedef struct hexo_calib hexo_calib;
+hexo_status hexo_calib_create(hexo_ctx *ctx, double S, double r, const double *taus, const uint32_t *counts,
+                              const double *strikes, uint32_t n_chains, double trunc_precision, hexo_calib **out);
+uint32_t hexo_calib_observations(const hexo_calib *c);
+hexo_status hexo_calib_prices(hexo_calib *c, const double *p /* 5 */, double *x);
+hexo_status hexo_calib_jacobian(hexo_calib *c, const double *p /* 5 */, double *jac);
+hexo_status hexo_calib_destroy(hexo_calib *c);
+
 /* --------------------------------------------------------------- shards */
 
 /* Exact partial sums over paths [path_lo, path_hi) of one request: for each

@@ -62,3 +62,61 @@ def test_gpu_matches_oracle_dynamic(engine, oracle):
         for (gp, gg), (wp, wg) in zip(out, want):
             np.testing.assert_allclose(gp, wp, rtol=0, atol=1e-10)
             np.testing.assert_allclose(gg, wg, rtol=0, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_calibration_callbacks_match_oracle(engine, oracle):
+    g, p, chains = _golden()
+    cal = engine.calibration(g["S"], g["r"], chains)
+    x = cal.prices(g["params5"])
+    jac = cal.jacobian(g["params5"])
+    want_x, want_j = [], []
+    for T, K in chains:
+        sp = oracle.swift_params(g["params5"], T, g["r"], g["S"], K.min(), K.max())
+        wp, wg = oracle.swift_price(g["params5"], T, g["r"], g["S"], K, sp, grad=True)
+        want_x.append(wp)
+        want_j.append(wg)
+    np.testing.assert_allclose(x, np.concatenate(want_x), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(jac, np.concatenate(want_j), rtol=0, atol=1e-10)
+    cal.close()
+
+
+def _levenberg_marquardt(f, jac, p0, x_obs, iters=100):
+    """A plain Levenberg-Marquardt loop (levmar's damping: mu starts at
+    1e-3 max diag(J'J), halved... on success, doubled on failure)."""
+    p = np.array(p0, dtype=float)
+    r = x_obs - f(p)
+    J = jac(p)
+    A = J.T @ J
+    mu = 1e-3 * A.diagonal().max()
+    for _ in range(iters):
+        gvec = J.T @ r
+        if np.abs(gvec).max() < 1e-10:
+            break
+        dp = np.linalg.solve(A + mu * np.eye(5), gvec)
+        if np.linalg.norm(dp) < 1e-10 * (np.linalg.norm(p) + 1e-10):
+            break
+        pn = p + dp
+        ok = pn[0] > 0 and pn[1] > 0 and abs(pn[2]) < 1 and pn[3] > 0 and pn[4] > 0
+        rn = x_obs - f(pn) if ok else None
+        if ok and np.all(np.isfinite(rn)) and rn @ rn < r @ r:
+            p, r = pn, rn
+            J = jac(p)
+            A = J.T @ J
+            mu *= 1.0 / 3.0
+        else:
+            mu *= 2.0
+    return p
+
+
+@pytest.mark.gpu
+def test_calibration_recovers_parameters(engine):
+    # the reference's levmar_test (src/UnitTest.cpp:480-509): prices at p,
+    # start from p + 0.2 in every component, recover p within 1e-2 (sum)
+    g, p, chains = _golden()
+    cal = engine.calibration(g["S"], g["r"], chains)
+    p_true = np.array(g["params5"])
+    x_obs = cal.prices(p_true)
+    got = _levenberg_marquardt(cal.prices, cal.jacobian, p_true + 0.2, x_obs)
+    assert np.abs(got - p_true).sum() < 1e-2, got
+    cal.close()
