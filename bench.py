@@ -331,6 +331,9 @@ def run_engine(args, rank, world, local):
         if args.autotune:
             reqs, cfg = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale)
             out["autotune"] = {"workload": f"{WORKLOAD}_paths_x{args.path_scale:g}", **eng.autotune(reqs, cfg)}
+            reqs, cfg = W.uneven_batch(seed=2, precision=FP64, path_scale=args.path_scale / 4)
+            out["autotune_fp64"] = {"workload": f"uneven_batch_64sets_fp64_paths_x{args.path_scale / 4:g}",
+                                    **eng.autotune(reqs, cfg)}
         eng.close()
         return out if rank == 0 else None
     if world > 1:

@@ -194,7 +194,7 @@ double cum4(const HP &p, double t) {
 
 // ------------------------------------------------------------------ kernels
 
-constexpr uint32_t kMaxJ = 2048;
+constexpr uint32_t kMaxJ = 1u << 16;
 
 struct Exp {                 // one expiry of one request
     HP p;
@@ -396,7 +396,7 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
                 if (s != HEXO_OK) return ctx_fail(ctx, s, "swift: the truncation loop did not converge");
             }
             if (!valid_params(sp))
-                return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "swift: J must be a power of two up to 2048 with k2 - k1 < 4J");
+                return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "swift: J must be a power of two up to 65536 with k2 - k1 < 4J");
             Exp e{};
             e.p = hp;
             e.tau = ch.tau;

@@ -47,7 +47,7 @@ extern "C" hexo_status hexo_autotune(hexo_ctx *ctx, const hexo_request *reqs, ui
                                      hexo_tune_entry *entries, uint32_t max_entries) {
     if (!ctx || !cfg || !reqs || n_reqs == 0) return HEXO_ERR_INVALID;
     const bool f32 = cfg->precision == HEXO_FP32;
-    const uint32_t blocks[3] = {128, 256, 512}, ppts[3] = {1, 2, 4}, unrolls[3] = {1, 2, 4};
+    const uint32_t blocks[5] = {128, 192, 256, 384, 512}, ppts[3] = {1, 2, 4}, unrolls[3] = {1, 2, 4};
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     cudaEvent_t e0 = nullptr, e1 = nullptr;

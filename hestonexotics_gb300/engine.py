@@ -397,8 +397,8 @@ class Engine:
         arr, keep, outputs = self._requests(requests)
         c = cfg.c()
         res = L.hexo_tune_result()
-        entries = (L.hexo_tune_entry * 27)()
-        self._check(self._lib.hexo_autotune(self._ctx, arr, len(requests), C.byref(c), C.byref(res), entries, 27))
+        entries = (L.hexo_tune_entry * 45)()
+        self._check(self._lib.hexo_autotune(self._ctx, arr, len(requests), C.byref(c), C.byref(res), entries, 45))
         table = [(entries[i].block, entries[i].paths_per_thread, entries[i].unroll, entries[i].ms)
                  for i in range(res.n_tried)]
         return {"block": res.block, "paths_per_thread": res.paths_per_thread, "unroll": res.unroll,

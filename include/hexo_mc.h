@@ -240,7 +240,7 @@ typedef struct hexo_swift_params {
     double sqrt_exp2_m;
     double lower, upper;      /* integration range of the log-price */
     int32_t k1, k2;           /* sum range */
-    uint32_t J, reserved;     /* frequencies (a power of two, at most 2048); reserved = 0 */
+    uint32_t J, reserved;     /* frequencies (a power of two, at most 65536); reserved = 0 */
 } hexo_swift_params;
 
 /* Host-only: the reference's dynamic choice of the parameters for one expiry
@@ -367,7 +367,7 @@ typedef struct hexo_tune_entry {
     float ms;
 } hexo_tune_entry;
 
-/* Sweeps threads per CTA {128,256,512} x paths per thread {1,2,4} x step
+/* Sweeps threads per CTA {128,192,256,384,512} x paths per thread {1,2,4} x step
  * unroll {1,2,4} (shapes that do not fit an SM are skipped) on the given
  * requests, times one launch of each, and makes the fastest the context's
  * shape for cfg->precision (saved to the context's autotune cache file when
