@@ -48,17 +48,17 @@ struct PathVars {
 // One QE step of one path (HSimulation.tpp:52-86), FP64.
 __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, double theta, dev::Shishua &g,
                                         dev::RngLane &c, const dev::Ring &r) {
+    const dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const double v = pv.v;
     const double m = __fma_rn(__dsub_rn(v, theta), sg.disc, theta);         // tpp:59
     const double sp2 = fabs(__fma_rn(v, sg.cA, sg.cB));                      // tpp:60
     const double mm = __dmul_rn(m, m);
     const bool quad = sp2 < __dmul_rn(1.5, mm);                              // Psi < PSI_C, tpp:61,63
-    float z1f = 0.0f;                                                        // draw order, tpp:67,72,80
+    float z1f = 0.0f, z2f;                                                   // draw order, tpp:67,72,80
     uint64_t uw = 0;
-    if (quad) z1f = dev::rng_next_g<false>(g, c, r);
-    else uw = dev::rng_next_u(g, c, r);
+    dev::draw_commit<false>(g, c, r, dp, quad, z1f, uw, z2f);
     const double z1 = (double)z1f;
-    const double z2 = (double)dev::rng_next_g<false>(g, c, r);
+    const double z2 = (double)z2f;
     double vn;
     if (quad) {                                                              // tpp:64-68
         const double inv = __ddiv_rn(__dmul_rn(2.0, mm), sp2);               // 2/Psi
@@ -90,6 +90,7 @@ __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, 
 // reference's tpp:59-60), everything else in float.
 __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
                                         const dev::Ring &r, float S0, float rr) {
+    const dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const ds::F2 v = pv.vd;
     const ds::F2 m = ds::fma(v, ds::F2{sg.ds_disc[0], sg.ds_disc[1]}, ds::F2{sg.ds_m0[0], sg.ds_m0[1]});
     const ds::F2 sp2 = ds::fma(v, ds::F2{sg.ds_cA[0], sg.ds_cA[1]}, ds::F2{sg.ds_cB[0], sg.ds_cB[1]});
@@ -98,11 +99,9 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
     const float t15 = __fmul_rn(1.5f, mm.h);
     const bool quad = fabsf(__fsub_rn(sp2.h, t15)) > __fmul_rn(0x1p-20f, sp2.h) ? sp2.h < t15
                                                                                  : ds::less(sp2, ds::mul_f(mm, 1.5f));
-    float z1 = 0.0f;
+    float z1 = 0.0f, z2;
     uint64_t uw = 0;
-    if (quad) z1 = dev::rng_next_g<true>(g, c, r);
-    else uw = dev::rng_next_u(g, c, r);
-    const float z2 = dev::rng_next_g<true>(g, c, r);
+    dev::draw_commit<true>(g, c, r, dp, quad, z1, uw, z2);
     ds::F2 vn;
     if (quad) {
         const ds::F2 inv = ds::div(ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)}, sp2);   // 2/Psi
