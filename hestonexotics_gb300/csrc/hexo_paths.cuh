@@ -116,9 +116,12 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
         const float Psi = __fdividef(sp2.h, mm.h);
         const float pp1 = __fadd_rn(Psi, 1.0f);
         const float p = __fdividef(__fsub_rn(Psi, 1.0f), pp1);
-        const double Ud = dev::uniform_f64(uw);                    // FP64 pipe: idle in this form
-        const float U = __double2float_rn(Ud);
-        const float omU = __double2float_rn(__dsub_rn(1.0, Ud));
+        // U = w 2^-64 and 1 - U = (~w + 1) 2^-64 to float accuracy from the two
+        // 32-bit halves (the FP64 form uses the exact double; a float-size
+        // difference moves p < U only when p is within 2^-24 of U)
+        const uint32_t whi = (uint32_t)(uw >> 32), wlo = (uint32_t)uw;
+        const float U = __fmaf_rn(__uint2float_rn(wlo), 0x1p-64f, __fmul_rn(__uint2float_rn(whi), 0x1p-32f));
+        const float omU = __fmaf_rn(__uint2float_rn(~wlo), 0x1p-64f, __fmul_rn(__uint2float_rn(~whi), 0x1p-32f));
         // v = log((1-p)/(1-U)) / beta with 1-p = 2/(Psi+1), 1/beta = m (Psi+1) / 2; never below 0
         const float lr = __logf(__fdividef(__fdividef(2.0f, pp1), omU));
         vn = ds::F2{p < U ? fmaxf(0.0f, __fmul_rn(__fmul_rn(__fmul_rn(0.5f, m.h), pp1), lr)) : 0.0f, 0.0f};

@@ -69,6 +69,8 @@ typedef struct hexo_ctx_opts {
 } hexo_ctx_opts;
 
 hexo_status hexo_ctx_create(hexo_ctx **out, const hexo_ctx_opts *opts /* NULL = defaults */);
+/* Waits for the context's work and frees it.  Batches, servers and
+ * calibration handles made on the context must be destroyed first. */
 hexo_status hexo_ctx_destroy(hexo_ctx *ctx);
 /* Copies the message of the last failure on this context into buf. */
 hexo_status hexo_ctx_last_error(hexo_ctx *ctx, char *buf, size_t buf_len);
