@@ -227,23 +227,17 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         for (uint32_t si = 0; si < td.seg_count; ++si) {
             const SegDesc sg = a.segs[S.seg_begin + si];
             const R hdt = kF32 ? (R)sg.f_hdt : (R)sg.hdt;
-            // all steps but the last: step, then trapezoid with this width
+            // every step, then the trapezoid with this width except after the
+            // last (pricing) step; one copy of the step code
 #pragma unroll UNROLL
-            for (uint32_t st = 1; st < sg.n_steps; ++st) {
+            for (uint32_t st = 1; st <= sg.n_steps; ++st) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
                     dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
                     if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf);
                     else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
-                    pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
+                    if (st < sg.n_steps) pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
                 }
-            }
-            // the pricing step
-#pragma unroll
-            for (int p = 0; p < PPT; ++p) {
-                dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
-                if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf);
-                else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
             }
             for (uint32_t mj = sg.mat_begin; mj < sg.mat_end; ++mj) {
                 const MatDesc M = a.mats[S.mat_begin + mj];
