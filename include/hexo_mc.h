@@ -45,7 +45,7 @@ typedef enum hexo_status {
     HEXO_ERR_INVALID = 1,      /* bad argument (NaN parameter, T <= 0, zero paths, ...) */
     HEXO_ERR_CUDA = 2,         /* a CUDA runtime call failed */
     HEXO_ERR_NOMEM = 3,        /* device or host allocation failed */
-    HEXO_ERR_UNSUPPORTED = 4,  /* valid but not supported by this build (e.g. rng_block_words != 16) */
+    HEXO_ERR_UNSUPPORTED = 4,  /* valid but not supported by the library (e.g. rng_block_words != 16) */
     HEXO_ERR_TIMEOUT = 5,      /* a bounded wait ran out */
     HEXO_ERR_NUMERIC = 6,      /* a payoff was not finite or exceeded the fixed-point range */
     HEXO_ERR_NOT_FOUND = 7,    /* unknown ticket */
