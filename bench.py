@@ -58,11 +58,11 @@ WORKLOAD = "uneven_batch_64sets_fp32_graph"
 ALG_FP32_OPS_PER_PATH_STEP = 102.0
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
-# Nsight Compute capture of this workload at 1/16 of its paths (130.2 MB +
-# 88.9 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
+# Nsight Compute capture of this workload at 1/16 of its paths (129.4 MB +
+# 84.0 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
 # traffic is the CTA-private sum slots a launch touches plus the descriptors;
 # it does not grow with the path count, so it is reported unscaled.
-PATHS_KERNEL_DRAM_BYTES = 130.2e6 + 88.9e6
+PATHS_KERNEL_DRAM_BYTES = 129.4e6 + 84.0e6
 
 
 def dist_env():
