@@ -9,12 +9,12 @@ namespace hexo {
 
 // Dynamic shared memory of the path kernel: per path two raw slots (16 x u64)
 // and two normal slots (16 x f32); per warp the conversion queue
-// (kWarpScratchBytes); the 64-option staging window of the payoff sums
-// (16-byte aligned).
+// (kWarpScratchBytes) and a 64-option window of 32-bit payoff sums (16-byte
+// aligned).
 inline size_t paths_smem_bytes(uint32_t block, uint32_t ppt) {
     const size_t rings = (size_t)ppt * 2 * kRngWords * block * (sizeof(uint64_t) + sizeof(float)) +
                          (size_t)(block / 32) * kWarpScratchBytes;
-    return (rings + 15) / 16 * 16 + 64u * kLimbs * sizeof(unsigned long long);
+    return (rings + 15) / 16 * 16 + (size_t)(block / 32) * 64u * kLimbs * sizeof(uint32_t);
 }
 
 // nullptr when (ppt, unroll) is not instantiated.

@@ -146,12 +146,14 @@ __device__ __forceinline__ double fma_r(double a, double b, double c) { return _
 // A CTA takes one tile (blockDim * PPT consecutive paths) at a time, so its
 // warps read the same set's descriptors (shared through L1); thread t holds
 // paths begin + p * blockDim + t.  A tile prices its set's options in
-// increasing (maturity-sorted) index order; warp sums are staged in a shared
-// window of kWindow consecutive options (shared-memory atomics) and flushed to
-// this CTA's private copy of the global sums only when an option falls past
-// the window and at the end of the tile, so the warps meet at a barrier a few
-// times per tile rather than at every maturity (measured: 12 % faster on the
-// uneven batch than a flush per maturity).
+// increasing (maturity-sorted) index order.  Each warp's sums (redux.sync)
+// are stored, without atomics, in the warp's own window of kWindow
+// consecutive options (one 32-bit value per option and limb, written once per
+// tile); the windows are summed and flushed to this CTA's private copy of the
+// global sums only when an option falls past the window and at the end of the
+// tile, so the warps meet at a barrier a few times per tile rather than at
+// every maturity (measured on the uneven batch: 12 % faster than a flush per
+// maturity; the per-warp windows another 4 %, 17 % on a 100-strike chain).
 constexpr uint32_t kWindow = 64;
 
 template <bool kF32, int PPT, int UNROLL>
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     uint64_t *raw_all = reinterpret_cast<uint64_t *>(smem_raw);
     float *nrm_all = reinterpret_cast<float *>(raw_all + (size_t)PPT * 2 * kRngWords * bd);
     uint16_t *tq_i_all = reinterpret_cast<uint16_t *>(nrm_all + (size_t)PPT * 2 * kRngWords * bd);
-    unsigned long long *win = reinterpret_cast<unsigned long long *>(
+    uint32_t *win = reinterpret_cast<uint32_t *>(
         smem_raw + ((size_t)PPT * 2 * kRngWords * bd * 12 + (size_t)(bd >> 5) * kWarpScratchBytes + 15) / 16 * 16);
 
     dev::Ring ring[PPT];
@@ -181,16 +183,21 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     __shared__ uint32_t s_tile;
     // this CTA's private copy of the sums: CTAs never contend for one address
     unsigned long long *const acc = a.acc + (size_t)(blockIdx.x % a.n_slots) * a.acc_slot_stride;
-    for (uint32_t i = tid; i < kWindow * kLimbs; i += bd) win[i] = 0ull;
-    // adds the window's sums for set options [base, base + kWindow) to the global copy and clears it
+    const uint32_t n_warps = bd >> 5;
+    for (uint32_t i = tid; i < n_warps * kWindow * kLimbs; i += bd) win[i] = 0u;
+    uint32_t *const wwin = win + warp * kWindow * kLimbs;   // this warp's window: one u32 per option and limb
+    // adds the warps' window sums for set options [base, base + kWindow) to the global copy and clears them
     auto flush = [&](const SetDesc &S, uint32_t base) {
         __syncthreads();
         for (uint32_t i = tid; i < kWindow * kLimbs; i += bd) {
-            const unsigned long long v = win[i];
+            unsigned long long v = 0ull;
+            for (uint32_t w = 0; w < n_warps; ++w) {
+                v += win[w * kWindow * kLimbs + i];
+                win[w * kWindow * kLimbs + i] = 0u;
+            }
             if (v != 0ull) {
                 const OptDesc &O = a.opts[S.opt_begin + base + i / kLimbs];
                 atomicAdd(&acc[(size_t)O.out_index * kLimbs + i % kLimbs], v);
-                win[i] = 0ull;
             }
         }
         __syncthreads();
@@ -284,12 +291,13 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                         }
                     }
                     if (!ok) atomicOr(a.error, 1);
-                    unsigned long long *slot = &win[(oi - win_base) * kLimbs];
+                    uint32_t mine = 0u;
 #pragma unroll
                     for (int x = 0; x < kLimbs; ++x) {
                         const uint32_t sum = __reduce_add_sync(0xffffffffu, l[x]);
-                        if (lane == 0 && sum != 0u) atomicAdd(&slot[x], (unsigned long long)sum);
+                        if (lane == (uint32_t)x) mine = sum;
                     }
+                    if (lane < (uint32_t)kLimbs) wwin[(oi - win_base) * kLimbs + lane] = mine;   // once per option and tile
                 }
             }
             const R hda = kF32 ? (R)sg.f_hdt_after : (R)sg.hdt_after;
