@@ -13,6 +13,8 @@
 // template instantiation.
 #pragma once
 
+#include <stdint.h>
+
 namespace hexo {
 namespace ds {
 
@@ -113,6 +115,59 @@ __device__ __forceinline__ F2 sqrt(F2 x) {
 }
 // x < y
 __device__ __forceinline__ bool less(F2 x, F2 y) { return x.h < y.h || (x.h == y.h && x.l < y.l); }
+
+// N 2^-64 for an integer 0 < N < 2^64: the top 24 bits (exact) and the next
+// 24 (rounded) of N.
+__device__ __forceinline__ F2 from_u64_2m64(uint64_t N) {
+    const uint32_t lz = (uint32_t)__clzll((long long)N);
+    const uint64_t n = N << lz;                           // msb at bit 63
+    const float sh = __uint_as_float((103u - lz) << 23);  // 2^(-24 - lz)
+    const float sl = __uint_as_float((79u - lz) << 23);   // 2^(-48 - lz)
+    const float h = __fmul_rn(__uint2float_rz((uint32_t)(n >> 40)), sh);
+    const float l = __fmul_rn(__uint2float_rn((uint32_t)(n >> 16) & 0x00ffffffu), sl);
+    return F2{h, l};
+}
+
+// Natural logarithm in double-single, for x >= 2^-126 (normal x.h).  The
+// reduction x = 2^k c_j (1 + r) with c_j = 1 + (j + 1/2)/128 from a table of
+// 1/c_j and log c_j (double-single, built by log_table_init), |r| <= 2^-8,
+// and log(1 + r) = r - r^2/2 + r^3/3 - r^4/4 + r^5/5 (the neglected terms are
+// below 2^-50): the square in double-single, the rest in float.  About 2^-46
+// absolute error for x near 1, relative beyond.
+struct LogTab {
+    float inv_h, inv_l, log_h, log_l;
+};
+constexpr uint32_t kLogTab = 128;
+
+__device__ __forceinline__ void log_table_init(LogTab *t, uint32_t tid, uint32_t nthreads) {
+    for (uint32_t j = tid; j < kLogTab; j += nthreads) {
+        const double c = 1.0 + ((double)j + 0.5) / (double)kLogTab;
+        const double ic = 1.0 / c, lc = ::log(c);
+        const float ih = __double2float_rn(ic), lh = __double2float_rn(lc);
+        t[j] = LogTab{ih, __double2float_rn(ic - (double)ih), lh, __double2float_rn(lc - (double)lh)};
+    }
+}
+
+__device__ __forceinline__ F2 log(F2 x, const LogTab *t) {
+    const uint32_t b = __float_as_uint(x.h);
+    const int k = (int)(b >> 23) - 127;
+    const uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+    const float M = __uint_as_float(mb);                                        // x.h 2^-k in [1, 2)
+    const float ls = __fmul_rn(x.l, __uint_as_float((uint32_t)(127 - k) << 23));  // x.l 2^-k
+    const uint32_t j = (mb >> 16) & (kLogTab - 1u);
+    const float c = __uint_as_float(0x3f800000u | (j << 16) | (1u << 15));      // c_j
+    const LogTab e = t[j];
+    const F2 r = mul(two_sum(__fsub_rn(M, c), ls), F2{e.inv_h, e.inv_l});
+    const float p2 = __fmul_rn(r.h, r.h);
+    const float e2 = __fmaf_rn(__fadd_rn(r.h, r.h), r.l, __fmaf_rn(r.h, r.h, -p2));
+    float poly = __fmaf_rn(r.h, 0.2f, -0.25f);
+    poly = __fmaf_rn(r.h, poly, 0x1.555556p-2f);
+    poly = __fmul_rn(__fmul_rn(p2, r.h), poly);                                 // r^3/3 - r^4/4 + r^5/5
+    F2 l1 = add(r, F2{__fmul_rn(-0.5f, p2), __fmul_rn(-0.5f, e2)});
+    l1 = add_f(l1, poly);
+    const F2 kl = mul_f(F2{0x1.62e430p-1f, -0x1.05c610p-29f}, (float)k);       // k ln 2
+    return add(add(kl, F2{e.log_h, e.log_l}), l1);
+}
 
 } // namespace ds
 } // namespace hexo

@@ -10,11 +10,11 @@ namespace hexo {
 // Dynamic shared memory of the path kernel: per path two raw slots (16 x u64)
 // and two normal slots (16 x f32); per warp the conversion queue
 // (kWarpScratchBytes) and a 64-option window of 32-bit payoff sums (16-byte
-// aligned).
+// aligned); the 128-entry double-single log table (2 KB).
 inline size_t paths_smem_bytes(uint32_t block, uint32_t ppt) {
     const size_t rings = (size_t)ppt * 2 * kRngWords * block * (sizeof(uint64_t) + sizeof(float)) +
                          (size_t)(block / 32) * kWarpScratchBytes;
-    return (rings + 15) / 16 * 16 + (size_t)(block / 32) * 64u * kLimbs * sizeof(uint32_t);
+    return (rings + 15) / 16 * 16 + (size_t)(block / 32) * 64u * kLimbs * sizeof(uint32_t) + 128u * 16u;
 }
 
 // nullptr when (ppt, unroll) is not instantiated.

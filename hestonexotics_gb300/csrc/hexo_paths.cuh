@@ -89,7 +89,7 @@ __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, 
 // double-single (m = v disc + m0 and s^2 = v cA + cB, algebraically the
 // reference's tpp:59-60), everything else in float.
 __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
-                                        const dev::Ring &r, float S0, float rr) {
+                                        const dev::Ring &r, float S0, float rr, const ds::LogTab *ltab) {
     const dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const ds::F2 v = pv.vd;
     const ds::F2 m = ds::fma(v, ds::F2{sg.ds_disc[0], sg.ds_disc[1]}, ds::F2{sg.ds_m0[0], sg.ds_m0[1]});
@@ -116,15 +116,31 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
         const float Psi = __fdividef(sp2.h, mm.h);
         const float pp1 = __fadd_rn(Psi, 1.0f);
         const float p = __fdividef(__fsub_rn(Psi, 1.0f), pp1);
-        // U = w 2^-64 and 1 - U = (~w + 1) 2^-64 to float accuracy from the two
-        // 32-bit halves (the FP64 form uses the exact double; a float-size
-        // difference moves p < U only when p is within 2^-24 of U)
+        // U = w 2^-64 to float accuracy from the two 32-bit halves
         const uint32_t whi = (uint32_t)(uw >> 32), wlo = (uint32_t)uw;
         const float U = __fmaf_rn(__uint2float_rn(wlo), 0x1p-64f, __fmul_rn(__uint2float_rn(whi), 0x1p-32f));
-        const float omU = __fmaf_rn(__uint2float_rn(~wlo), 0x1p-64f, __fmul_rn(__uint2float_rn(~whi), 0x1p-32f));
-        // v = log((1-p)/(1-U)) / beta with 1-p = 2/(Psi+1), 1/beta = m (Psi+1) / 2; never below 0
-        const float lr = __logf(__fdividef(__fdividef(2.0f, pp1), omU));
-        vn = ds::F2{p < U ? fmaxf(0.0f, __fmul_rn(__fmul_rn(__fmul_rn(0.5f, m.h), pp1), lr)) : 0.0f, 0.0f};
+        // p < U sends the variance to 0 or not: decided in float when the two
+        // are further apart than float error (2^-19 relative), else exactly as
+        // the FP64 form decides it (rare: a few 1e-5 of these steps), so that
+        // the path does not take the other branch than in FP64
+        bool take = p < U;
+        if (fabsf(__fsub_rn(p, U)) <= __fmul_rn(0x1p-17f, __fadd_rn(p, U))) {
+            const double Pd = __ddiv_rn(__dadd_rn((double)sp2.h, (double)sp2.l), __dadd_rn((double)mm.h, (double)mm.l));
+            take = __ddiv_rn(__dsub_rn(Pd, 1.0), __dadd_rn(Pd, 1.0)) < dev::uniform_f64(uw);
+        }
+        // v = log((1-p)/(1-U)) / beta, in double-single like the quadratic
+        // branch (a float-size error here would move later branch decisions):
+        // 1 - p = 2 m^2 / (s^2 + m^2), 1/beta = m (s^2 + m^2) / (2 m^2), and
+        // 1 - U = (2^64 - w) 2^-64 from the whole word
+        vn = ds::F2{0.0f, 0.0f};
+        if (take) {
+            const ds::F2 spm = ds::add(sp2, mm);
+            const ds::F2 mm2 = ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)};
+            const ds::F2 x = ds::div(mm2, ds::mul(spm, ds::from_u64_2m64(0ull - uw)));
+            const ds::F2 v1 = ds::mul(ds::div(ds::mul(m, spm), mm2), ds::log(x, ltab));
+            if (v1.h > 0.0f) vn = v1;
+        }
+        (void)pp1;
     }
     pv.vd = vn;
     pv.v = vn.h;
@@ -167,6 +183,9 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     uint16_t *tq_i_all = reinterpret_cast<uint16_t *>(nrm_all + (size_t)PPT * 2 * kRngWords * bd);
     uint32_t *win = reinterpret_cast<uint32_t *>(
         smem_raw + ((size_t)PPT * 2 * kRngWords * bd * 12 + (size_t)(bd >> 5) * kWarpScratchBytes + 15) / 16 * 16);
+    // double-single log table of the FP32 form's exponential branch, after the windows
+    ds::LogTab *ltab = reinterpret_cast<ds::LogTab *>(win + (size_t)(bd >> 5) * kWindow * kLimbs);
+    if constexpr (kF32) ds::log_table_init(ltab, tid, bd);   // visible after the first tile's barrier
 
     dev::Ring ring[PPT];
     dev::WarpScratch ws[PPT];
@@ -243,7 +262,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
                     dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
-                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf);
+                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
                     else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
                     if (st < sg.n_steps) pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
                 }
