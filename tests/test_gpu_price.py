@@ -105,6 +105,17 @@ def test_fp32_vs_fp64_oracle(engine, oracle, maker):
     fp32_check(p32, se32, p64, req.S0)
 
 
+def test_fp32_vs_fp64_every_set_of_the_uneven_batch(engine):
+    # all 64 parameter sets (high vol-of-vol ones included), 1/32 of the paths:
+    # the FP32 form against the FP64 form on the same streams
+    reqs, cfg32 = W.uneven_batch(seed=2, precision=E.FP32, path_scale=1 / 32)
+    cfg64 = E.Config(**{**cfg32.__dict__, "precision": E.FP64})
+    o32 = engine.price_batch(reqs, cfg32)
+    o64 = engine.price_batch(reqs, cfg64)
+    for rq, (p32, se32), (p64, _) in zip(reqs, o32, o64):
+        fp32_check(p32, se32, p64, rq.S0)
+
+
 def test_launch_shapes_bit_identical(engine):
     req, cfg = W.single_chain(n_paths=5000)
     cfg.steps_per_year = 52.0
