@@ -128,12 +128,12 @@ __device__ __forceinline__ F2 from_u64_2m64(uint64_t N) {
     return F2{h, l};
 }
 
-// Natural logarithm in double-single, for x >= 2^-126 (normal x.h).  The
+// Natural logarithm in double-single.  The
 // reduction x = 2^k c_j (1 + r) with c_j = 1 + (j + 1/2)/128 from a table of
 // 1/c_j and log c_j (double-single, built by log_table_init), |r| <= 2^-8,
 // and log(1 + r) = r - r^2/2 + r^3/3 - r^4/4 + r^5/5 (the neglected terms are
 // below 2^-50): the square in double-single, the rest in float.  About 2^-46
-// absolute error for x near 1, relative beyond.
+// absolute error for x near 1, relative beyond; x > 0 normal.
 struct LogTab {
     float inv_h, inv_l, log_h, log_l;
 };
@@ -157,14 +157,17 @@ __device__ __forceinline__ F2 log(F2 x, const LogTab *t) {
     const uint32_t j = (mb >> 16) & (kLogTab - 1u);
     const float c = __uint_as_float(0x3f800000u | (j << 16) | (1u << 15));      // c_j
     const LogTab e = t[j];
-    const F2 r = mul(two_sum(__fsub_rn(M, c), ls), F2{e.inv_h, e.inv_l});
+    // r = ((M - c_j) + ls) / c_j: M - c_j is exact, ls below 2^-23 of M
+    F2 r = mul_f(F2{e.inv_h, e.inv_l}, __fsub_rn(M, c));
+    r.l = __fmaf_rn(ls, e.inv_h, r.l);
     const float p2 = __fmul_rn(r.h, r.h);
     const float e2 = __fmaf_rn(__fadd_rn(r.h, r.h), r.l, __fmaf_rn(r.h, r.h, -p2));
     float poly = __fmaf_rn(r.h, 0.2f, -0.25f);
     poly = __fmaf_rn(r.h, poly, 0x1.555556p-2f);
     poly = __fmul_rn(__fmul_rn(p2, r.h), poly);                                 // r^3/3 - r^4/4 + r^5/5
-    F2 l1 = add(r, F2{__fmul_rn(-0.5f, p2), __fmul_rn(-0.5f, e2)});
-    l1 = add_f(l1, poly);
+    // r - r^2/2 + poly, with |r^2/2| <= 2^-9 |r|: one ordered sum and the small terms
+    const F2 s1 = fast_two_sum(r.h, __fmul_rn(-0.5f, p2));
+    const F2 l1 = fast_two_sum(s1.h, __fadd_rn(__fadd_rn(s1.l, r.l), __fmaf_rn(-0.5f, e2, poly)));
     const F2 kl = mul_f(F2{0x1.62e430p-1f, -0x1.05c610p-29f}, (float)k);       // k ln 2
     return add(add(kl, F2{e.log_h, e.log_l}), l1);
 }

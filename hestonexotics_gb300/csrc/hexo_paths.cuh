@@ -129,15 +129,13 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
             take = __ddiv_rn(__dsub_rn(Pd, 1.0), __dadd_rn(Pd, 1.0)) < dev::uniform_f64(uw);
         }
         // v = log((1-p)/(1-U)) / beta, in double-single like the quadratic
-        // branch (a float-size error here would move later branch decisions):
-        // 1 - p = 2 m^2 / (s^2 + m^2), 1/beta = m (s^2 + m^2) / (2 m^2), and
-        // 1 - U = (2^64 - w) 2^-64 from the whole word
+        // branch (a float-size error here would move later branch decisions).
+        // With Y = (s^2 + m^2) / (2 m^2) = 1/(1-p) = 1/(beta m):
+        // v = -m Y log(Y (1 - U)), 1 - U = (2^64 - w) 2^-64 from the whole word
         vn = ds::F2{0.0f, 0.0f};
         if (take) {
-            const ds::F2 spm = ds::add(sp2, mm);
-            const ds::F2 mm2 = ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)};
-            const ds::F2 x = ds::div(mm2, ds::mul(spm, ds::from_u64_2m64(0ull - uw)));
-            const ds::F2 v1 = ds::mul(ds::div(ds::mul(m, spm), mm2), ds::log(x, ltab));
+            const ds::F2 Y = ds::div(ds::add(sp2, mm), ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)});
+            const ds::F2 v1 = ds::mul(ds::mul(m, Y), ds::neg(ds::log(ds::mul(Y, ds::from_u64_2m64(0ull - uw)), ltab)));
             if (v1.h > 0.0f) vn = v1;
         }
         (void)pp1;
