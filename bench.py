@@ -58,11 +58,11 @@ WORKLOAD = "uneven_batch_64sets_fp32_graph"
 ALG_FP32_OPS_PER_PATH_STEP = 102.0
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
-# Nsight Compute capture of this workload at 1/16 of its paths (129.4 MB +
-# 84.0 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
+# Nsight Compute capture of this workload at 1/16 of its paths (129.0 MB +
+# 85.9 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
 # traffic is the CTA-private sum slots a launch touches plus the descriptors;
 # it does not grow with the path count, so it is reported unscaled.
-PATHS_KERNEL_DRAM_BYTES = 129.4e6 + 84.0e6
+PATHS_KERNEL_DRAM_BYTES = 129.0e6 + 85.9e6
 
 
 def dist_env():
@@ -419,8 +419,8 @@ def run_engine(args, rank, world, local):
             n_opts += len(pa)
 
         # every set of the batch at 1/16 of its paths: FP32 against FP64 on the same streams
-        reqs16, cfg16 = W.uneven_batch(seed=2, precision=FP32, path_scale=1 / 16)
-        cfg16_64 = W.uneven_batch(seed=2, precision=FP64, path_scale=1 / 16)[1]
+        reqs16, cfg16 = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale / 16)
+        cfg16_64 = W.uneven_batch(seed=2, precision=FP64, path_scale=args.path_scale / 16)[1]
         o32 = eng.price_batch(reqs16, cfg16)
         o64 = eng.price_batch(reqs16, cfg16_64)
         all_rel, all_in_se, all_n, all_big = 0.0, 0, 0, 0
