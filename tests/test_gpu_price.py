@@ -230,3 +230,44 @@ def test_invalid_request_errors(engine):
     assert ei.value.status == 1
     with pytest.raises(HexoError):
         engine.price(params, 100.0, E.Options(np.array([100.0]), 1.0, 0), E.Config(block=100))
+
+
+EDGE_SETS = [
+    # v0, theta, rho, kappa, sigma, r: the ends of the admissible ranges
+    (0.04, 0.04, -1.0, 1.5, 0.5, 0.02),     # rho = -1: the spot noise has no own part (K3 = 0)
+    (0.04, 0.04, 1.0, 1.5, 0.5, 0.02),      # rho = +1
+    (0.0, 0.04, -0.7, 1.5, 0.5, 0.02),      # v0 = 0
+    (0.04, 0.04, -0.7, 1.5, 0.01, 0.02),    # sigma -> 0: always the quadratic branch
+    (0.04, 0.04, -0.7, 1.5, 2.0, 0.02),     # sigma = 2: mostly the exponential branch
+    (0.04, 0.04, -0.7, 20.0, 0.5, 0.0),     # fast mean reversion
+    (0.04, 0.04, -0.7, 0.01, 0.5, 0.05),    # slow mean reversion
+    (0.09, 1e-4, -0.5, 2.0, 0.3, 0.0),      # theta -> 0
+]
+
+
+@pytest.mark.parametrize("k", range(len(EDGE_SETS)))
+def test_parameter_edges_fp64_vs_oracle_and_fp32(engine, oracle, k):
+    v0, th, rho, kap, sig, r = EDGE_SETS[k]
+    params = E.Params(v0, th, rho, kap, sig, r)
+    S0 = 100.0
+    T = np.repeat([1 / 52, 0.5, 2.0], 4)
+    K = np.tile([50.0, 95.0, 105.0, 400.0], 3)   # deep in and far out of the money included
+    kinds = np.tile([E.ASIAN, E.EUROPEAN], 6).astype(np.uint32)
+    req = E.Request(params, S0, E.Options(K, T, kinds), seed=11)
+    cfg = E.Config(n_paths=1 << 12, step_mode=E.STEP_GRID, steps_per_year=252.0, seed=11, precision=E.FP64)
+    p64, _ = engine.price(params, S0, req.options, E.Config(**{**cfg.__dict__, "seed": 11}))
+    op, _, _ = oracle_price(oracle, req, cfg)
+    assert_fp64_close(p64, op, S0)
+    p32, se32 = engine.price(params, S0, req.options, E.Config(**{**cfg.__dict__, "precision": E.FP32}))
+    fp32_check(p32, se32, p64, S0)
+
+
+def test_extreme_spot_levels(engine, oracle):
+    for S0 in (1e-3, 1e4):
+        params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5, 0.02)
+        K = S0 * np.array([0.8, 1.0, 1.2])
+        req = E.Request(params, S0, E.Options(K, 1.0, E.ASIAN), seed=3)
+        cfg = E.Config(n_paths=1 << 12, steps=63, seed=3, precision=E.FP64)
+        p64, _ = engine.price(params, S0, req.options, E.Config(**{**cfg.__dict__}))
+        op, _, _ = oracle_price(oracle, req, cfg)
+        assert_fp64_close(p64, op, S0)
