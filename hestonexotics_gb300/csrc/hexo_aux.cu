@@ -107,6 +107,15 @@ __global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *ou
     }
 }
 
+__global__ void dbg_limbs_kernel(const double *pay, uint64_t n, bool f32, uint32_t *out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
+        const bool ok = f32 ? dev::limbs_add_f32((float)pay[i], l) : dev::limbs_add_f64(pay[i], l);
+        for (int x = 0; x < kLimbs; ++x) out[i * kLimbs + x] = ok ? l[x] : 0xFFFFFFFFu;
+    }
+}
+
 cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st) {
     dbg_words_kernel<<<(n_streams + 127) / 128, 128, 0, st>>>(seed, n_streams, n_words, out);
     return cudaGetLastError();
@@ -117,6 +126,12 @@ cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *k
     const uint32_t bd = 64;
     const size_t smem = (size_t)2 * kRngWords * bd * (sizeof(uint64_t) + sizeof(float)) + (bd / 32) * kWarpScratchBytes;
     dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, n_streams, kinds, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, uint32_t *out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    dbg_limbs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pay, n, f32, out);
     return cudaGetLastError();
 }
 

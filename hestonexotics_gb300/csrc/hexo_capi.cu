@@ -561,6 +561,24 @@ hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n,
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug normals");
 }
 
+hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision,
+                                    uint32_t *out) {
+    if (!ctx || !pay || !out || n == 0) return HEXO_ERR_INVALID;
+    if (precision != HEXO_FP64 && precision != HEXO_FP32) return ctx_fail(ctx, HEXO_ERR_INVALID, "unknown precision");
+    std::lock_guard<std::mutex> lk(ctx->run_mu);
+    cudaSetDevice(ctx->device);
+    DevBuf dp, dout;
+    cudaError_t e = dp.alloc(n * sizeof(double));
+    if (e == cudaSuccess) e = dout.alloc(n * kLimbs * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dp.p, pay, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_dbg_limbs((const double *)dp.p, n, precision == HEXO_FP32, (uint32_t *)dout.p, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, dout.p, n * kLimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug payoff limbs");
+}
+
 hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out4) {
     if (!ctx || !out4) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);

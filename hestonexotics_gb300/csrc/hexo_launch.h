@@ -37,6 +37,7 @@ cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words
 cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
                              cudaStream_t st);
 cudaError_t launch_dbg_normals(const uint64_t *words, uint64_t n, double *out, cudaStream_t st);
+cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, uint32_t *out, cudaStream_t st);
 cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4);
 
 } // namespace hexo

@@ -170,6 +170,46 @@ __device__ __forceinline__ double fma_r(double a, double b, double c) { return _
 // maturity; the per-warp windows another 4 %, 17 % on a 100-strike chain).
 constexpr uint32_t kWindow = 64;
 
+// Folds the call payoffs (AsianContract.h:43-47, VanillaContract.h:37-39) of
+// option oi of this warp's paths into the warp's window entry wslot: exact
+// limbs per path, one warp sum per limb (redux.sync), stored by lane 0.  A
+// warp whose payoffs are all 0 leaves its (cleared) window entry as it is.
+template <bool kF32, int PPT>
+__device__ __forceinline__ void fold_option(const KernelArgs &a, const SetDesc &S, uint32_t oi, uint32_t *wslot,
+                                            uint32_t lane, const bool (&active)[PPT], const uint64_t (&kpath)[PPT],
+                                            const typename Real<kF32>::T (&asian)[PPT],
+                                            const typename Real<kF32>::T (&euro)[PPT]) {
+    const OptDesc &O = a.opts[S.opt_begin + oi];
+    uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
+    bool ok = true, any = false;
+#pragma unroll
+    for (int p = 0; p < PPT; ++p) {
+        if (active[p] && kpath[p] < O.n_paths) {
+            if constexpr (kF32) {
+                const float pay = fmaxf(0.0f, __fsub_rn(O.kind == 0 ? asian[p] : euro[p], O.f_strike));
+                any |= pay != 0.0f;
+                ok &= dev::limbs_add_f32(pay, l);
+            } else {
+                const double pay = fmax(0.0, __dsub_rn(O.kind == 0 ? asian[p] : euro[p], O.strike));
+                any |= pay != 0.0;
+                ok &= dev::limbs_add_f64(pay, l);
+            }
+        }
+    }
+    if (!ok) atomicOr(a.error, 1);
+    if (__any_sync(0xffffffffu, any)) {
+        uint32_t sum[kLimbs];
+#pragma unroll
+        for (int x = 0; x < kLimbs; ++x) sum[x] = __reduce_add_sync(0xffffffffu, l[x]);
+        if (lane == 0u) {   // once per option and tile; 8-byte aligned (24 B per option)
+            uint2 *w = reinterpret_cast<uint2 *>(wslot);
+            w[0] = make_uint2(sum[0], sum[1]);
+            w[1] = make_uint2(sum[2], sum[3]);
+            w[2] = make_uint2(sum[4], sum[5]);
+        }
+    }
+}
+
 template <bool kF32, int PPT, int UNROLL>
 __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     typedef typename Real<kF32>::T R;
@@ -285,36 +325,13 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                         a.dbg_euro[at] = (double)euro[p];
                     }
                 }
-                // payoffs of the maturity's options: exact limbs, a warp sum per
-                // limb (redux.sync), staged in the shared window
+                // payoffs of the maturity's options, staged in the warp's window
                 for (uint32_t oi = M.opt_begin; oi < M.opt_end; ++oi) {
                     if (oi >= win_base + kWindow) {           // CTA-uniform: all warps price the same options
                         flush(S, win_base);
                         win_base = oi - oi % kWindow;
                     }
-                    const OptDesc O = a.opts[S.opt_begin + oi];
-                    uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
-                    bool ok = true;
-#pragma unroll
-                    for (int p = 0; p < PPT; ++p) {
-                        if (active[p] && kpath[p] < O.n_paths) {
-                            if constexpr (kF32) {
-                                const float f = O.kind == 0 ? asian[p] : euro[p];
-                                ok &= dev::limbs_add_f32(fmaxf(0.0f, __fsub_rn(f, O.f_strike)), l);
-                            } else {
-                                const double f = O.kind == 0 ? asian[p] : euro[p];
-                                ok &= dev::limbs_add_f64(fmax(0.0, __dsub_rn(f, O.strike)), l);   // AsianContract.h:43-47
-                            }
-                        }
-                    }
-                    if (!ok) atomicOr(a.error, 1);
-                    uint32_t mine = 0u;
-#pragma unroll
-                    for (int x = 0; x < kLimbs; ++x) {
-                        const uint32_t sum = __reduce_add_sync(0xffffffffu, l[x]);
-                        if (lane == (uint32_t)x) mine = sum;
-                    }
-                    if (lane < (uint32_t)kLimbs) wwin[(oi - win_base) * kLimbs + lane] = mine;   // once per option and tile
+                    fold_option<kF32, PPT>(a, S, oi, wwin + (oi - win_base) * kLimbs, lane, active, kpath, asian, euro);
                 }
             }
             const R hda = kF32 ? (R)sg.f_hdt_after : (R)sg.hdt_after;

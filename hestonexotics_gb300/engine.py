@@ -423,6 +423,14 @@ class Engine:
         self._check(self._lib.hexo_debug_normals(self._ctx, _u64p(words), len(words), _dp(out)))
         return out
 
+    def payoff_limbs(self, pay: np.ndarray, precision: int) -> np.ndarray:
+        """The kernels' 25-bit limbs of round(pay 2^40) and round(pay^2 2^24), [n, 6]."""
+        pay = np.ascontiguousarray(pay, dtype=np.float64)
+        out = np.zeros(len(pay) * 6, dtype=np.uint32)
+        self._check(self._lib.hexo_debug_payoff_limbs(self._ctx, _dp(pay), len(pay), precision,
+                                                      out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out.reshape(len(pay), 6)
+
     def pipe_peaks(self) -> dict:
         out = np.zeros(4)
         self._check(self._lib.hexo_debug_pipe_peaks(self._ctx, _dp(out)))

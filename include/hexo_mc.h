@@ -388,6 +388,14 @@ hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t n_stream
                                  uint32_t n, double *out);
 /* AS241 of u = (double)w / (double)UINT64_MAX for each word: out[i]. */
 hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n, double *out);
+/* The fixed-point split of payoffs as the path kernels fold them: for each
+ * pay[i] (converted to float first when precision is HEXO_FP32) the six
+ * 25-bit limbs out[6*i .. 6*i+5] of q = round(pay * 2^40) and
+ * q2 = round(pay^2 * 2^24), ties to even (pay^2 rounded to double in the
+ * FP64 form, exact in the FP32 form); all six are 0xFFFFFFFF for a payoff
+ * the kernels reject (not finite, negative or >= 2^23). */
+hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision,
+                                    uint32_t *out);
 /* Measured lane-operation rates (per second) of this GPU's pipes, from
  * throughput probes: out4 = {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD}. */
 hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out4);
