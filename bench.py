@@ -14,8 +14,10 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              (planning, upload, run and result download inside the timing)
   fp64       the plain FP64 form, one request per launch, on a sample of the
              sets, and the FP32 form's error against it
-  roofline   the path kernel's algorithmic FP32-pipe operations per second
-             against this GPU's measured FP32-FMA lane rate
+  roofline   the path kernel's algorithmic operations per second on the pipe
+             that binds (FP32 FMA, MUFU or integer ALU, each against this
+             GPU's lane rate measured in the run), with the branch mix p_Q
+             the kernel counted
   serving    Poisson request streams through the continuous-batching server
              (FP32), p50/p99 submit-to-completion latency, against the same
              streams priced one request per plain FP64 launch
@@ -48,14 +50,28 @@ METRIC = "Heston path-steps/s, 1 GB300: batched FP32 vs plain FP64 at ≤1e-4 re
 UNIT = "path-steps/s"
 WORKLOAD = "uneven_batch_64sets_fp32_graph"
 
-# Algorithmic FP32-pipe operations per path-step of the scheme (QE step,
-# trapezoid, two float32 AS241 evaluations), counted from the reference
-# operation order: QE 3 (m) + 2 (s^2) + 1 (m^2) + 7 (quadratic branch)
-# + 9 (log-spot) + 1 (time) + 3 (Asian) = 26; AS241 central branch per
-# normal: 2 (R) + 28 (two Horner chains) + 2 (Q*num/den) + 3 (Q from u)
-# = 35, two normals per step = 70.  Divides, square roots, exp and log
-# count once each (6 per step).  Total 102.
-ALG_FP32_OPS_PER_PATH_STEP = 102.0
+# Algorithmic operations per path-step of the scheme, by the pipe that
+# executes them in the FP32 form, counted in the reference's operation order
+# (HSimulation.tpp:52-86, as241.f90, RNG.cpp) with p = the measured share of
+# quadratic-branch steps, n_N = 1 + p normals and 1 - p uniforms per step,
+# and c = 0.85 the share of AS241 draws on its central branch:
+#   FP32 FMA pipe: QE 3 (m) + 2 (s^2) + 1 (m^2) + 7 p (quadratic branch)
+#     + 5 (1 - p) (exponential branch) + 9 (log-spot) + 1 (time) + 3 (Asian)
+#     = 24 + 2 p; AS241 5 + 31 = 36 per normal;
+#   MUFU (XU): divides 5 - 2 p (QE) + n_N (AS241); square roots 1 + 2 p
+#     + n_N (1 - c); exp 1, log 1 - p + n_N (1 - c); 2 word conversions;
+#   INT ALU: SHISHUA, 122 shift/logic/add operations per 16-word block,
+#     2 words per step.
+AS241_CENTRAL = 0.85
+SHISHUA_ALU_PER_WORD = 122.0 / 16.0
+
+
+def alg_ops_per_path_step(p: float) -> dict:
+    n_n = 1.0 + p
+    tail = n_n * (1.0 - AS241_CENTRAL)
+    return {"fp32_fma": 24.0 + 2.0 * p + 36.0 * n_n,
+            "mufu": (5.0 - 2.0 * p + n_n) + (1.0 + 2.0 * p + tail) + 1.0 + (1.0 - p + tail) + 2.0,
+            "int32_alu": 2.0 * SHISHUA_ALU_PER_WORD}
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
 # Nsight Compute capture of this workload at 1/16 of its paths (129.0 MB +
@@ -370,7 +386,9 @@ def run_engine(args, rank, world, local):
             ev[k][1].record(stream)
         batch.collect()
         step_ms.append(ev[k][0].elapsed_time(ev[k][1]))
-        kernel_ms.append(batch.info()["last_kernel_ms"])
+        last = batch.info()
+        kernel_ms.append(last["last_kernel_ms"])
+    p_quad = last["quad_steps"] / max(1, last["executed_path_steps"])   # branch mix the kernel counted
     barrier()
     clk = clocks.stop()
     total_ms = sum(step_ms)
@@ -434,8 +452,15 @@ def run_engine(args, rank, world, local):
 
         peaks = eng.pipe_peaks()
         kms = statistics.mean(kernel_ms)
-        achieved = ALG_FP32_OPS_PER_PATH_STEP * nominal / (kms * 1e-3) / 1e9
-        peak = peaks["fp32_fma"] / 1e9
+        # per pipe: the path-steps/s its measured peak allows; the smallest binds
+        ops = alg_ops_per_path_step(p_quad)
+        rate = nominal / (kms * 1e-3)
+        pipes = {k: {"ops_per_path_step": ops[k], "peak_lane_ops_per_s": peaks[k],
+                     "bound_path_steps_per_s": peaks[k] / ops[k], "frac": rate / (peaks[k] / ops[k])}
+                 for k in ops}
+        bind = min(pipes, key=lambda k: pipes[k]["bound_path_steps_per_s"])
+        achieved = ops[bind] * rate / 1e9
+        peak = peaks[bind] / 1e9
         serving = None
         if args.serve_rates:
             rates = [float(x) for x in args.serve_rates.split(",") if x]
@@ -465,14 +490,14 @@ def run_engine(args, rank, world, local):
                            "all_64_sets_at_1_16_paths": {"fp32_vs_fp64_max_rel_err": all_rel,
                                                          "options_checked": all_big,
                                                          "fp32_within_1se_frac": all_in_se / max(1, all_n)}},
-            "roofline": {"bound": "compute: FP32 pipe (no tensor-core or HBM bound on this path)",
-                         "achieved": achieved, "peak": peak, "unit": "Gop/s (FP32-pipe lane ops)",
+            "roofline": {"bound": f"compute: {bind} pipe (no tensor-core or HBM bound on this path)",
+                         "achieved": achieved, "peak": peak, "unit": f"Gop/s ({bind} lane ops)",
                          "frac": achieved / peak, "traffic": PATHS_KERNEL_DRAM_BYTES,
                          "traffic_note": "DRAM bytes per launch from ncu at 1/16 of the paths; sum slots and "
                                          "descriptors, independent of the path count",
-                         "peak_source": "FP32-FMA lane rate measured in this run by hexo_debug_pipe_peaks",
-                         "alg_ops_per_path_step": ALG_FP32_OPS_PER_PATH_STEP, "kernel_ms": kms,
-                         "pipe_peaks_lane_ops_per_s": peaks},
+                         "peak_source": "lane rates measured in this run by hexo_debug_pipe_peaks (of measured)",
+                         "p_quadratic": p_quad, "as241_central_share": AS241_CENTRAL,
+                         "pipes": pipes, "kernel_ms": kms, "pipe_peaks_lane_ops_per_s": peaks},
             "serving": serving,
             "cpu_baseline": cpu,
             "clocks": clk,

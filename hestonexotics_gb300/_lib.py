@@ -66,7 +66,7 @@ class hexo_batch_info(C.Structure):
                 ("n_tiles", C.c_uint32), ("n_sets", C.c_uint32), ("n_options", C.c_uint32), ("block", C.c_uint32),
                 ("paths_per_thread", C.c_uint32), ("unroll", C.c_uint32), ("grid", C.c_uint32),
                 ("device_bytes", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
-                ("last_kernel_ms", C.c_double)]
+                ("last_kernel_ms", C.c_double), ("quad_steps", C.c_uint64)]
 
 
 class hexo_plan_stats(C.Structure):

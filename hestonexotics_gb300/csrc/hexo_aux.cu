@@ -188,21 +188,38 @@ __global__ void peak_mufu_kernel(int iters, float *sink) {
     if (s == -1.0f) sink[0] = s;
 }
 
-__global__ void peak_int_kernel(int iters, unsigned *sink) {
+// The multiplier is a launch argument: with a compile-time constant the
+// compiler composes unrolled links of the affine chain into one.
+__global__ void peak_int_kernel(int iters, unsigned mul, unsigned *sink) {
     unsigned a[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 2654435761u + j;
     for (int i = 0; i < iters; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) a[j] = a[j] * 1664525u + 1013904223u;
+        for (int j = 0; j < 8; ++j) a[j] = a[j] * mul + 1013904223u;
     unsigned s = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) s ^= a[j];
     if (s == 0xFFFFFFFFu) sink[0] = s;
 }
 
-// Lane operations per second for {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD}.
-cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4) {
+// Two ALU-pipe operations per link: a funnel-shift rotate and an xor.
+__global__ void peak_alu_kernel(int iters, unsigned *sink) {
+    unsigned a[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 2654435761u + j;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = __funnelshift_l(a[j], a[j], 7) ^ 0x9e3779b9u;
+    unsigned s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s ^= a[j];
+    if (s == 0xFFFFFFFFu) sink[0] = s;
+}
+
+// Lane operations per second for {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD,
+// INT32 ALU (shift, logic)}.
+cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out5) {
     void *sink = nullptr;
     cudaError_t e = cudaMalloc(&sink, 64);
     if (e != cudaSuccess) return e;
@@ -210,8 +227,9 @@ cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     const int threads = 256, blocks = sm_count * 8;
-    const int iters[4] = {4096, 256, 1024, 4096};
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+    const int iters[5] = {4096, 256, 1024, 4096, 4096};
+    const double ops[5] = {1.0, 1.0, 1.0, 1.0, 2.0};   // lane operations per link
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
         float ms = 0.f;
         for (int rep = 0; rep < 2; ++rep) {   // first launch warms up
             cudaEventRecord(a, st);
@@ -219,14 +237,15 @@ cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4) {
             case 0: peak_ffma_kernel<<<blocks, threads, 0, st>>>(iters[k], (float *)sink); break;
             case 1: peak_dfma_kernel<<<blocks, threads, 0, st>>>(iters[k], (double *)sink); break;
             case 2: peak_mufu_kernel<<<blocks, threads, 0, st>>>(iters[k], (float *)sink); break;
-            case 3: peak_int_kernel<<<blocks, threads, 0, st>>>(iters[k], (unsigned *)sink); break;
+            case 3: peak_int_kernel<<<blocks, threads, 0, st>>>(iters[k], 1664525u, (unsigned *)sink); break;
+            case 4: peak_alu_kernel<<<blocks, threads, 0, st>>>(iters[k], (unsigned *)sink); break;
             }
             cudaEventRecord(b, st);
             e = cudaEventSynchronize(b);
             if (e != cudaSuccess) break;
             cudaEventElapsedTime(&ms, a, b);
         }
-        out4[k] = (double)blocks * threads * iters[k] * 8.0 / (ms * 1e-3);
+        out5[k] = (double)blocks * threads * iters[k] * 8.0 * ops[k] / (ms * 1e-3);
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);

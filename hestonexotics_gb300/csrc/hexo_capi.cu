@@ -98,7 +98,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_acc_sum = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_price = take(n_out * sizeof(double));
     const size_t o_se = take(n_out * sizeof(double));
-    const size_t o_ctl = take(2 * sizeof(uint32_t));   // queue head, error flags
+    const size_t o_ctl = take(kCtlBytes);   // queue head, error flags, quadratic-branch steps
     db.bytes = off;
     cudaError_t e = cudaSuccess;
     if (db.dmem == nullptr || db.dcap < db.bytes) {
@@ -113,7 +113,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t h_price = hoff; hoff = align_up(hoff + n_out * sizeof(double), 64);
     const size_t h_se = hoff; hoff = align_up(hoff + n_out * sizeof(double), 64);
     const size_t h_acc = hoff; hoff = align_up(hoff + (size_t)n_out * kLimbs * sizeof(unsigned long long), 64);
-    const size_t h_ctl = hoff; hoff = align_up(hoff + 2 * sizeof(uint32_t), 64);
+    const size_t h_ctl = hoff; hoff = align_up(hoff + kCtlBytes, 64);
     if (db.hmem == nullptr || db.hcap < hoff) {
         db.hmem = nullptr;
         db.own_h = true;
@@ -142,6 +142,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     db.d_acc_sum = reinterpret_cast<unsigned long long *>(d + o_acc_sum);
     a.queue = reinterpret_cast<unsigned int *>(d + o_ctl);
     a.error = reinterpret_cast<int *>(d + o_ctl + sizeof(uint32_t));
+    a.quad_steps = reinterpret_cast<unsigned long long *>(d + o_ctl + 2 * sizeof(uint32_t));
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
     db.d_disc = reinterpret_cast<double *>(d + o_disc);
     db.d_price = reinterpret_cast<double *>(d + o_price);
@@ -177,7 +178,7 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     if ((e = cudaMemsetAsync(db.args.acc, 0, (size_t)db.n_slots * n_out * kLimbs * sizeof(unsigned long long), st)) !=
         cudaSuccess)
         return e;
-    if ((e = cudaMemsetAsync(db.args.queue, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(db.args.queue, 0, kCtlBytes, st)) != cudaSuccess) return e;
     // inside a stream capture the timing events become event-record nodes of the graph
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if ((e = cudaStreamIsCapturing(st, &cap)) != cudaSuccess) return e;
@@ -194,7 +195,7 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     if (copy_acc)
         if ((e = cudaMemcpyAsync(db.h_acc, db.d_acc_sum, (size_t)n_out * kLimbs * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-    return cudaMemcpyAsync(db.h_ctl, db.args.queue, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    return cudaMemcpyAsync(db.h_ctl, db.args.queue, kCtlBytes, cudaMemcpyDeviceToHost, st);
 }
 
 hexo_status batch_wait(DeviceBatch &db) {
@@ -413,9 +414,10 @@ hexo_status hexo_batch_info_get(hexo_batch *b, hexo_batch_info *info) {
     info->grid = b->db.grid;
     info->device_bytes = b->db.bytes;
     info->h2d_bytes = b->db.h2d_bytes;
-    info->d2h_bytes = (uint64_t)bp.n_out * 2 * sizeof(double) + 2 * sizeof(uint32_t);
+    info->d2h_bytes = (uint64_t)bp.n_out * 2 * sizeof(double) + kCtlBytes;
     float ms = 0.0f;
     info->last_kernel_ms = cudaEventElapsedTime(&ms, b->db.ev_k0, b->db.ev_k1) == cudaSuccess ? (double)ms : -1.0;
+    std::memcpy(&info->quad_steps, b->db.h_ctl + 2, sizeof(uint64_t));
     return HEXO_OK;
 }
 
@@ -579,11 +581,11 @@ hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug payoff limbs");
 }
 
-hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out4) {
-    if (!ctx || !out4) return HEXO_ERR_INVALID;
+hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out5) {
+    if (!ctx || !out5) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
-    cudaError_t e = measure_pipe_peaks((int)ctx->sm_count, ctx->stream, out4);
+    cudaError_t e = measure_pipe_peaks((int)ctx->sm_count, ctx->stream, out5);
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "pipe peaks");
 }
 

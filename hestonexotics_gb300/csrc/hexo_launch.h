@@ -38,6 +38,6 @@ cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *k
                              cudaStream_t st);
 cudaError_t launch_dbg_normals(const uint64_t *words, uint64_t n, double *out, cudaStream_t st);
 cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, uint32_t *out, cudaStream_t st);
-cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out4);
+cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out5);
 
 } // namespace hexo

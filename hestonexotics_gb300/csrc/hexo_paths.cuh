@@ -45,8 +45,9 @@ struct PathVars {
 // different template instantiations: every launch shape computes the same
 // bits for the same path.
 
-// One QE step of one path (HSimulation.tpp:52-86), FP64.
-__device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, double theta, dev::Shishua &g,
+// One QE step of one path (HSimulation.tpp:52-86), FP64; returns whether it
+// took the quadratic branch.
+__device__ __forceinline__ bool qe_step(PathVars<false> &pv, const SegDesc &sg, double theta, dev::Shishua &g,
                                         dev::RngLane &c, const dev::Ring &r) {
     const dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const double v = pv.v;
@@ -83,12 +84,14 @@ __device__ __forceinline__ void qe_step(PathVars<false> &pv, const SegDesc &sg, 
     pv.lx = __fma_rn(sd, z2, t);
     pv.Xp = pv.X;
     pv.X = exp(pv.lx);                                                       // tpp:82
+    return quad;
 }
 
 // One QE step, FP32 form: the same scheme and draws; the variance in
 // double-single (m = v disc + m0 and s^2 = v cA + cB, algebraically the
-// reference's tpp:59-60), everything else in float.
-__device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
+// reference's tpp:59-60), everything else in float; returns whether it took
+// the quadratic branch.
+__device__ __forceinline__ bool qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
                                         const dev::Ring &r, float S0, float rr, const ds::LogTab *ltab) {
     const dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const ds::F2 v = pv.vd;
@@ -150,6 +153,7 @@ __device__ __forceinline__ void qe_step(PathVars<true> &pv, const SegDesc &sg, d
     pv.lx = __fadd_rn(pv.lx, inc);
     pv.Xp = pv.X;
     pv.X = __fmul_rn(S0, __expf(__fmaf_rn(rr, vn.h, pv.lx)));
+    return quad;
 }
 
 __device__ __forceinline__ float add_r(float a, float b) { return __fadd_rn(a, b); }
@@ -271,6 +275,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         const double theta = S.theta;
         const float S0f = S.f_S0, rf = S.f_r;
         uint32_t win_base = 0;   // first set option of the staging window
+        uint32_t n_quad = 0;     // this thread's quadratic-branch steps of active paths in the tile
 
         dev::Shishua g[PPT];
         dev::RngLane c[PPT];
@@ -300,8 +305,10 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
                     dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
-                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
-                    else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
+                    bool quad;
+                    if constexpr (kF32) quad = qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
+                    else quad = qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
+                    n_quad += (active[p] && quad) ? 1u : 0u;
                     if (st < sg.n_steps) pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
                 }
             }
@@ -339,6 +346,10 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             for (int p = 0; p < PPT; ++p) pv[p].acc = fma_r(hda, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
         }
         flush(S, win_base);
+        if (a.quad_steps != nullptr) {   // branch mix of the launch, one atomic per warp and tile
+            const uint32_t wq = __reduce_add_sync(0xffffffffu, n_quad);
+            if (lane == 0u && wq != 0u) atomicAdd(a.quad_steps, (unsigned long long)wq);
+        }
     }
 }
 

@@ -37,7 +37,7 @@ struct DeviceBatch {
     double *d_disc = nullptr, *d_price = nullptr, *d_se = nullptr;
     double *h_price = nullptr, *h_se = nullptr;
     unsigned long long *h_acc = nullptr;
-    uint32_t *h_ctl = nullptr;   // queue head, error flags
+    uint32_t *h_ctl = nullptr;   // control block of the last run (kCtlBytes): queue head, error flags, quad steps
     cudaGraphExec_t graph_exec = nullptr;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around the path kernel
     uint64_t h2d_bytes = 0;

@@ -432,9 +432,9 @@ class Engine:
         return out.reshape(len(pay), 6)
 
     def pipe_peaks(self) -> dict:
-        out = np.zeros(4)
+        out = np.zeros(5)
         self._check(self._lib.hexo_debug_pipe_peaks(self._ctx, _dp(out)))
-        return {"fp32_fma": out[0], "fp64_fma": out[1], "mufu": out[2], "int32": out[3]}
+        return {"fp32_fma": out[0], "fp64_fma": out[1], "mufu": out[2], "int32": out[3], "int32_alu": out[4]}
 
     def path_finals(self, params: Params, S0: float, options: Options, cfg: Config, path_lo: int, path_hi: int):
         n = path_hi - path_lo

@@ -168,6 +168,9 @@ typedef struct hexo_batch_info {
     uint64_t h2d_bytes;           /* bytes uploaded when the batch is planned (descriptors) */
     uint64_t d2h_bytes;           /* bytes copied back per run (prices, standard errors, status) */
     double last_kernel_ms;        /* path-kernel time of the last collected run (CUDA events) */
+    uint64_t quad_steps;          /* of the last collected run: QE steps that took the quadratic branch
+                                     (HSimulation.tpp:63-68); quad_steps / executed_path_steps is the
+                                     branch mix p_Q */
 } hexo_batch_info;
 
 hexo_status hexo_batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
@@ -397,8 +400,9 @@ hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n,
 hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision,
                                     uint32_t *out);
 /* Measured lane-operation rates (per second) of this GPU's pipes, from
- * throughput probes: out4 = {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD}. */
-hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out4);
+ * throughput probes: out5 = {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD,
+ * INT32 ALU (shift and logic)}. */
+hexo_status hexo_debug_pipe_peaks(hexo_ctx *ctx, double *out5);
 /* Per-path final values (Asian average, interpolated terminal spot) at every
  * distinct maturity for paths [path_lo, path_hi); NaN after a path's last
  * maturity.  Arrays are [(k - path_lo) * n_mats + j]; n_mats_out receives

@@ -27,7 +27,9 @@
  *                    accumulation `prices[i] += payoff/n` (tpp:40) kept in
  *                    path order but race-free (per-thread arrays).
  *   per-path driver: the stream partition the GPU engine uses: path k of a
- *                    request draws from its own RNG(block_words, seed+k).
+ *                    request draws from its own RNG(block_words, seed+k);
+ *                    oracle_branch_counts walks the same paths and counts
+ *                    the QE steps on the quadratic branch (tpp:63-68).
  *
  * Built twice by oracle/Makefile: liboracle.so (-O2 -ffp-contract=off, the
  * parity checker) and liboracle_fast.so (the reference's release flags minus
@@ -92,8 +94,9 @@ struct Params { double v0, theta, rho, kappa, sigma, r, q; };
 
 struct PathState { double Xc, Xp, vc, vp, t, tp, logX; };
 
-/* HSimulation.tpp:52-86 (+ drift in K_0) */
-inline void qe_step(PathState &st, const Params &p, double delta, OracleRNG &rng) {
+/* HSimulation.tpp:52-86 (+ drift in K_0); returns whether the step took the
+ * quadratic branch (Psi < 1.5, tpp:63). */
+inline bool qe_step(PathState &st, const Params &p, double delta, OracleRNG &rng) {
     const double v_0 = p.v0, theta = p.theta, rho = p.rho, kappa = p.kappa, eps = p.sigma;
     (void)v_0;
     const double gamma_1 = .5, gamma_2 = .5;
@@ -103,7 +106,8 @@ inline void qe_step(PathState &st, const Params &p, double delta, OracleRNG &rng
                            theta * eps * eps / (2 * kappa) * (1. - discount) * (1. - discount));
     double Psi = sp2 / (m * m);
     st.vp = st.vc;
-    if (Psi < 1.5) {
+    const bool quad = Psi < 1.5;
+    if (quad) {
         double bp2 = 2 / Psi - 1 + std::sqrt(2 / Psi * (2 / Psi - 1));
         double b = std::sqrt(bp2);
         double a = m / (1 + bp2);
@@ -125,6 +129,7 @@ inline void qe_step(PathState &st, const Params &p, double delta, OracleRNG &rng
     st.Xc = std::exp(st.logX);
     st.tp = st.t;
     st.t += delta;
+    return quad;
 }
 
 /* Maturity-grouped view of one pricing request. */
@@ -146,13 +151,15 @@ struct Problem {
  * for-increment takes after the last pricing (tpp:35), which matters only
  * when the stream is shared with the next path. */
 template <class Visit>
-inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&visit) {
+inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&visit, uint64_t *counts = nullptr) {
     PathState st{pr.S0, pr.S0, pr.p.v0, pr.p.v0, 0., 0., std::log(pr.S0)};
     const size_t m = pr.T.size();
     size_t j = 0;
+    uint64_t n_quad = 0, n_steps = 0;   // optional branch counts (counts[0], counts[1])
     double dt = pr.T[0] / pr.steps[0];  // update_earliest, AsianContract.h:35-38
     double acc = 0.;                    // reset, AsianContract.h:39-42
-    qe_step(st, pr.p, dt, rng);         // ++(heston_sde = initial_state), tpp:35
+    n_quad += qe_step(st, pr.p, dt, rng);   // ++(heston_sde = initial_state), tpp:35
+    ++n_steps;
     for (;;) {
         bool more = true;
         while (j < m && st.t >= pr.T[j]) {                              // tpp:36
@@ -167,10 +174,12 @@ inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&v
         }
         if (j >= m || !more) {
             if (trailing) qe_step(st, pr.p, dt, rng);                   // tpp:35 for-increment
+            if (counts) { counts[0] += n_quad; counts[1] += n_steps; }
             return;
         }
         acc += dt * .5 * (st.Xc + st.Xp);                               // AsianContract.h:25-28
-        qe_step(st, pr.p, dt, rng);
+        n_quad += qe_step(st, pr.p, dt, rng);
+        ++n_steps;
     }
 }
 
@@ -324,6 +333,46 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
         if (price) price[o] = disc * (double)mean;
         if (stderr_out) stderr_out[o] = n > 0 ? disc * std::sqrt((double)(var / n)) : 0.0;
     }
+    return 0;
+}
+
+/*
+ * Branch counts of the per-path partition: over paths [path_lo, path_hi),
+ * each walked to its last needed maturity as oracle_price_paths walks it,
+ * counts[0] = QE steps on the quadratic branch (HSimulation.tpp:63-68),
+ * counts[1] = all QE steps.  The GPU kernels report the same two numbers
+ * (the executed path-steps of a launch and its quadratic-branch steps).
+ */
+int oracle_branch_counts(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
+                         const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
+                         double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                         uint64_t path_hi, int n_threads, uint64_t *counts) {
+    Problem pr;
+    int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
+    if (rc) return rc;
+    if (block_words == 0 || (block_words * 8) % 128 != 0) return 4;  // RNG.cpp:10
+    std::vector<uint64_t> mat_paths(pr.T.size(), 0);
+    for (size_t j = 0; j < pr.T.size(); ++j)
+        for (uint32_t o : pr.opts[j]) mat_paths[j] = std::max(mat_paths[j], n_paths[o]);
+    const uint64_t n_max = *std::max_element(mat_paths.begin(), mat_paths.end());
+    path_hi = std::min(path_hi, n_max);
+    const int nt = n_threads > 0 ? n_threads : 1;
+    std::vector<uint64_t> part(2 * (size_t)nt, 0);
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+    for (int64_t k = (int64_t)path_lo; k < (int64_t)path_hi; ++k) {
+#ifdef _OPENMP
+        uint64_t *c = &part[2 * (size_t)omp_get_thread_num()];
+#else
+        uint64_t *c = &part[0];
+#endif
+        size_t last = 0;
+        for (size_t j = 0; j < pr.T.size(); ++j)
+            if (mat_paths[j] > (uint64_t)k) last = j;
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        run_path(pr, rng, false, [&](size_t j, double, double) { return j < last; }, c);
+    }
+    counts[0] = counts[1] = 0;
+    for (int t = 0; t < nt; ++t) { counts[0] += part[2 * (size_t)t]; counts[1] += part[2 * (size_t)t + 1]; }
     return 0;
 }
 

@@ -126,6 +126,23 @@ def price_paths(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, 
     return price, se, sums.reshape(n, 6)
 
 
+def branch_counts(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
+                  steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=None, threads=None):
+    """(quadratic-branch QE steps, all QE steps) of the per-path partition."""
+    strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
+    p = np.ascontiguousarray(params7, dtype=np.float64)
+    counts = np.zeros(2, dtype=np.uint64)
+    hi = int(n_paths.max()) if path_hi is None else int(path_hi)
+    th = threads or os.cpu_count() or 1
+    rc = lib().oracle_branch_counts(_p(p), C.c_double(S0), C.c_uint32(len(strike)), _p(strike), _p(T), _p(kind),
+                                    _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps), C.c_double(steps_per_year),
+                                    C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(block_words), C.c_uint64(path_lo),
+                                    C.c_uint64(hi), C.c_int(th), _p(counts))
+    if rc != 0:
+        raise ValueError(f"oracle_branch_counts failed: {rc}")
+    return int(counts[0]), int(counts[1])
+
+
 def path_finals(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
                 steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=64):
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)

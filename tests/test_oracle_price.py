@@ -89,3 +89,19 @@ def test_ragged_path_counts(oracle):
         if o == 0:
             assert np.array_equal(l1[0], limbs[0])
     assert np.all(price > 0)
+
+
+def test_branch_counts_walk_the_reference_step_count(oracle):
+    # T = 1 at 252 steps: the time sum in double stays below 1 after 252
+    # steps, so each path takes 253 (HSimulation.tpp:35-36); the quadratic
+    # share drops when the Feller condition is violated (more mass near 0)
+    base = [0.04, 0.04, -0.7, 1.5, 0.5, 0.0, 0.0]
+    feller = [0.04, 0.04, -0.9, 0.5, 1.0, 0.0, 0.0]
+    q, n = oracle.branch_counts(base, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42)
+    qf, nf = oracle.branch_counts(feller, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42)
+    assert n == nf == 512 * 253
+    assert 0.5 < q / n < 1.0 and 0.0 < qf / nf < q / n
+    # a path range splits the counts exactly
+    q1, n1 = oracle.branch_counts(base, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42, path_hi=200)
+    q2, n2 = oracle.branch_counts(base, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42, path_lo=200)
+    assert (q1 + q2, n1 + n2) == (q, n)
