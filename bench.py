@@ -26,7 +26,7 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              host cores) on a bounded sample of the same workload
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
-  python bench.py --precision-sweep | --swift | --autotune [--path-scale S]   (reports, not the benchmark)
+  python bench.py --precision-sweep | --swift | --configs | --autotune [--path-scale S]   (reports, not the benchmark)
 """
 from __future__ import annotations
 
@@ -280,6 +280,71 @@ def run_precision_sweep(eng, counts):
     return out
 
 
+# ------------------------------------------------------- single requests
+
+def run_configs_report(eng):
+    """The two single-request configurations: the plain Asian (S0 = K = 100,
+    T = 1, 252 reference steps, 65,536 paths, seed 42) and the single chain
+    (seed 1, 8 maturities x 50 strikes x Asian/European, 2^20 paths, daily
+    grid).  Per form: end-to-end path-steps/s of one hexo_price call (host
+    buffers in and out, median of 5 after a warm-up) and the path kernel's
+    own time; beside them the oracle port on all host cores with the same
+    per-path streams (median of 3), and, for the plain Asian, the port of
+    the reference's own thread partition (price()'s n / threads paths per
+    thread from one RNG(2^20, 1 << tid) each, HSimulation.tpp:23-29)."""
+    from oracle import oracle as O
+    from hestonexotics_gb300 import FP32, FP64
+    from hestonexotics_gb300 import workloads as W
+    O.build()
+    threads = os.cpu_count() or 1
+    out = []
+    for name, make in (("plain_asian_65536", lambda prec: W.plain_asian(n_paths=65536)),
+                       ("single_chain_seed1_2^20", lambda prec: W.single_chain(n_paths=1 << 20, precision=prec))):
+        row = {"config": name}
+        for tag, prec in (("fp64", FP64), ("fp32", FP32)):
+            rq, cfg = make(prec)
+            cfg.precision = prec
+            nominal = plan_stats([rq], cfg).nominal_path_steps
+            eng.price(rq.params, rq.S0, rq.options, cfg)
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                eng.price(rq.params, rq.S0, rq.options, cfg)
+                ts.append(time.perf_counter() - t0)
+            b = eng.prepare_batch([rq], cfg)
+            kms = []
+            for _ in range(4):
+                b.launch()
+                b.collect()
+                kms.append(b.info()["last_kernel_ms"])
+            b.close()
+            row[tag] = {"e2e_path_steps_per_s": nominal / statistics.median(ts),
+                        "e2e_ms": 1e3 * statistics.median(ts), "kernel_ms": min(kms[1:]),
+                        "kernel_path_steps_per_s": nominal / (min(kms[1:]) * 1e-3)}
+        rq, cfg = make(FP64)
+        row["nominal_path_steps"] = nominal
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            _oracle_price_fast(O, rq, cfg, threads)
+            ts.append(time.perf_counter() - t0)
+        row["cpu_port"] = {"path_steps_per_s": nominal / statistics.median(ts), "cores": threads,
+                           "seconds": statistics.median(ts)}
+        if name.startswith("plain_asian"):
+            o = rq.options
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                O.price_reference_partition(rq.params.as_array(), rq.S0, o.strike, o.T, o.payoff.astype(np.uint8),
+                                            cfg.steps, cfg.n_paths, n_threads=threads, omp_threads=threads,
+                                            fast=True)
+                ts.append(time.perf_counter() - t0)
+            row["cpu_reference_partition"] = {"path_steps_per_s": nominal / statistics.median(ts), "cores": threads,
+                                              "seconds": statistics.median(ts)}
+        out.append(row)
+    return out
+
+
 # ------------------------------------------------------------------ SWIFT
 
 def run_swift_report(eng, n_sets=1024):
@@ -337,13 +402,15 @@ def run_engine(args, rank, world, local):
     from hestonexotics_gb300 import workloads as W
 
     torch.cuda.set_device(local)
-    if args.precision_sweep or args.autotune or args.swift:
+    if args.precision_sweep or args.autotune or args.swift or args.configs:
         eng = Engine(local)
         out = {"metric": METRIC, "unit": UNIT}
         if args.precision_sweep:
             out["precision_sweep"] = run_precision_sweep(eng, [1 << k for k in (16, 18, 20, 22, 24)])
         if args.swift:
             out["swift"] = run_swift_report(eng)
+        if args.configs:
+            out["configs"] = run_configs_report(eng)
         if args.autotune:
             reqs, cfg = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale)
             out["autotune"] = {"workload": f"{WORKLOAD}_paths_x{args.path_scale:g}", **eng.autotune(reqs, cfg)}
@@ -542,6 +609,9 @@ def main():
                     help="instead of the benchmark: FP32 vs FP64 errors on the single chain at 2^16..2^24 paths")
     ap.add_argument("--swift", action="store_true",
                     help="instead of the benchmark: SWIFT pricer and calibration-callback timings")
+    ap.add_argument("--configs", action="store_true",
+                    help="instead of the benchmark: the plain Asian and the single chain as single requests, "
+                         "GPU both forms against the CPU port")
     ap.add_argument("--autotune", action="store_true",
                     help="instead of the benchmark: the launch-shape sweep on the uneven batch (use --path-scale)")
     ap.add_argument("--path-scale", type=float, default=1.0,
