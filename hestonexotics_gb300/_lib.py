@@ -178,6 +178,9 @@ PROTOTYPES = {
 _lib = None
 
 
+ABI_VERSION = 2   # HEXO_ABI_VERSION of include/hexo_mc.h these prototypes and structs follow
+
+
 def load() -> C.CDLL:
     """Loads libhexo_mc.so (built in-tree) and binds every prototype."""
     global _lib
@@ -192,6 +195,9 @@ def load() -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.hexo_abi_version() != ABI_VERSION:
+        raise EngineUnavailable(f"{LIB_PATH} has ABI version {lib.hexo_abi_version()}, these bindings "
+                                f"expect {ABI_VERSION}: rebuild it")
     _lib = lib
     return lib
 

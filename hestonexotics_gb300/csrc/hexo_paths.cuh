@@ -141,7 +141,6 @@ __device__ __forceinline__ bool qe_step(PathVars<true> &pv, const SegDesc &sg, d
             const ds::F2 v1 = ds::mul(ds::mul(m, Y), ds::neg(ds::log(ds::mul(Y, ds::from_u64_2m64(0ull - uw)), ltab)));
             if (v1.h > 0.0f) vn = v1;
         }
-        (void)pp1;
     }
     pv.vd = vn;
     pv.v = vn.h;

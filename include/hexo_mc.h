@@ -38,7 +38,10 @@
 extern "C" {
 #endif
 
-#define HEXO_ABI_VERSION 1u
+/* Raised whenever a struct's layout or a function's signature changes.
+ * 2: hexo_batch_info.quad_steps; hexo_debug_pipe_peaks fills five rates;
+ *    hexo_debug_payoff_limbs. */
+#define HEXO_ABI_VERSION 2u
 
 typedef enum hexo_status {
     HEXO_OK = 0,

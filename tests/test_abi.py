@@ -178,3 +178,8 @@ def test_host_finaliser_from_oracle_limbs(lib, oracle):
     fp, fse = E.finalize_limbs(p, opts, cfg, limbs)
     np.testing.assert_allclose(fp, price, rtol=1e-14)
     np.testing.assert_allclose(fse, se, rtol=1e-9)
+
+
+def test_abi_version_matches_header_and_bindings(lib):
+    m = re.search(r"#define\s+HEXO_ABI_VERSION\s+(\d+)u", HEADER.read_text())
+    assert m and int(m.group(1)) == L.ABI_VERSION == lib.hexo_abi_version()
