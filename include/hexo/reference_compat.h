@@ -86,6 +86,8 @@ inline hexo_ctx *compat_context() {
     static std::once_flag once;
     static hexo_ctx *ctx = nullptr;
     static hexo_status st = HEXO_OK;
+    if (hexo_abi_version() != HEXO_ABI_VERSION)
+        throw std::runtime_error("hexo: libhexo_mc.so was built for another version of hexo_mc.h");
     std::call_once(once, [] { st = hexo_ctx_create(&ctx, nullptr); });
     if (st != HEXO_OK || ctx == nullptr)
         throw std::runtime_error(std::string("hexo: cannot create engine context: ") + hexo_status_string(st));
