@@ -321,6 +321,22 @@ def run_configs_report(eng):
             row[tag] = {"e2e_path_steps_per_s": nominal / statistics.median(ts),
                         "e2e_ms": 1e3 * statistics.median(ts), "kernel_ms": min(kms[1:]),
                         "kernel_path_steps_per_s": nominal / (min(kms[1:]) * 1e-3)}
+            # the geometric control variate on the Asian options: same paths, smaller error
+            p_plain, se_plain = eng.price(rq.params, rq.S0, rq.options, cfg)
+            cfg.control_variate = 1
+            eng.price(rq.params, rq.S0, rq.options, cfg)
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                p_cv, se_cv = eng.price(rq.params, rq.S0, rq.options, cfg)
+                ts.append(time.perf_counter() - t0)
+            cfg.control_variate = 0
+            asian = (rq.options.payoff == 0) & (p_plain > 0.05)
+            ratio = float(np.median(se_plain[asian] / se_cv[asian])) if asian.any() else None
+            row[tag]["control_variate"] = {
+                "e2e_ms": 1e3 * statistics.median(ts), "asian_options": int(asian.sum()),
+                "median_se_ratio_plain_over_cv": ratio,
+                "paths_for_equal_error": (1.0 / ratio ** 2) if ratio else None}
         rq, cfg = make(FP64)
         row["nominal_path_steps"] = nominal
         ts = []

@@ -47,7 +47,7 @@ class hexo_mc_cfg(C.Structure):
     _fields_ = [("n_paths", C.c_uint64), ("step_mode", C.c_uint32), ("steps", C.c_uint32),
                 ("steps_per_year", C.c_double), ("seed", C.c_uint32), ("rng_block_words", C.c_uint32),
                 ("precision", C.c_uint32), ("block", C.c_uint32), ("paths_per_thread", C.c_uint32),
-                ("unroll", C.c_uint32)]
+                ("unroll", C.c_uint32), ("control_variate", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class hexo_ctx_opts(C.Structure):
@@ -178,7 +178,7 @@ PROTOTYPES = {
 _lib = None
 
 
-ABI_VERSION = 2   # HEXO_ABI_VERSION of include/hexo_mc.h these prototypes and structs follow
+ABI_VERSION = 3   # HEXO_ABI_VERSION of include/hexo_mc.h these prototypes and structs follow
 
 
 def load() -> C.CDLL:

@@ -7,7 +7,7 @@ namespace hexo {
 
 cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t smem, cudaStream_t st,
                          const KernelArgs &a) {
-    const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll);
+    const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll, sh.cv);
     if (fn == nullptr) return cudaErrorInvalidValue;
     KernelArgs args = a;
     void *params[] = {&args};
@@ -19,27 +19,43 @@ cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t 
 __global__ void finalize_kernel(const unsigned long long *__restrict__ acc, uint32_t n_slots, uint64_t slot_stride,
                                 const uint64_t *__restrict__ n_paths, const double *__restrict__ disc, uint32_t n,
                                 double *__restrict__ price, double *__restrict__ se,
-                                unsigned long long *__restrict__ acc_sum) {
+                                unsigned long long *__restrict__ acc_sum, const double *__restrict__ cv_eg,
+                                const uint32_t *__restrict__ cv_partner) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint64_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
-    for (uint32_t s = 0; s < n_slots; ++s)
+    auto total = [&](uint32_t o, uint64_t (&l)[kLimbs]) {
 #pragma unroll
-        for (int x = 0; x < kLimbs; ++x) l[x] += acc[(size_t)s * slot_stride + (size_t)i * kLimbs + x];
+        for (int x = 0; x < kLimbs; ++x) l[x] = 0;
+        for (uint32_t s = 0; s < n_slots; ++s)
+#pragma unroll
+            for (int x = 0; x < kLimbs; ++x) l[x] += acc[(size_t)s * slot_stride + (size_t)o * kLimbs + x];
+    };
+    uint64_t l[kLimbs];
+    total(i, l);
     if (acc_sum != nullptr)
 #pragma unroll
         for (int x = 0; x < kLimbs; ++x) acc_sum[(size_t)i * kLimbs + x] = l[x];
     double p, s;
-    finalize_limbs6(l, n_paths[i], disc[i], &p, &s);
+    const uint32_t g = cv_partner != nullptr ? cv_partner[i] : ~0u;
+    if (g != ~0u) {   // an Asian option with the control variate: its geometric and difference sums
+        uint64_t lg[kLimbs], ld[kLimbs];
+        total(g, lg);
+        total(g + 1u, ld);
+        finalize_cv(l, lg, ld, n_paths[i], disc[i], cv_eg[i], &p, &s);
+    } else {
+        finalize_limbs6(l, n_paths[i], disc[i], &p, &s);
+    }
     price[i] = p;
     se[i] = s;
 }
 
 cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
                             const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
-                            unsigned long long *acc_sum, cudaStream_t st) {
+                            unsigned long long *acc_sum, cudaStream_t st, const double *cv_eg,
+                            const uint32_t *cv_partner) {
     if (n == 0) return cudaSuccess;
-    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, n, price, se, acc_sum);
+    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, n, price, se, acc_sum,
+                                                      cv_eg, cv_partner);
     return cudaGetLastError();
 }
 

@@ -38,11 +38,16 @@ LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg) {
     if (cfg.block) sh.block = cfg.block;
     if (cfg.paths_per_thread) sh.ppt = cfg.paths_per_thread;
     if (cfg.unroll) sh.unroll = cfg.unroll;
+    if (cfg.control_variate) {   // its kernels run one path per thread, no unroll
+        sh.cv = true;
+        if (!cfg.paths_per_thread) sh.ppt = 1;
+        if (!cfg.unroll) sh.unroll = 1;
+    }
     return sh;
 }
 
 hexo_status shape_check(hexo_ctx *ctx, bool f32, const LaunchShape &sh, size_t &smem, uint32_t &ctas_per_sm) {
-    const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll);
+    const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll, sh.cv);
     if (fn == nullptr || sh.block == 0 || sh.block % 32 != 0 || sh.block > 512)
         return ctx_fail(ctx, HEXO_ERR_INVALID, "unsupported launch shape (block multiple of 32 up to 512, ppt/unroll in {1,2,4})");
     smem = paths_smem_bytes(sh.block, sh.ppt);
@@ -66,6 +71,8 @@ DeviceBatch::~DeviceBatch() {
     if (ev_k1) cudaEventDestroy(ev_k1);
     if (dmem && own_d) cudaFree(dmem);
     if (hmem && own_h) cudaFreeHost(hmem);
+    if (d_cv_eg) cudaFree(d_cv_eg);
+    if (d_cv_partner) cudaFree(d_cv_partner);
 }
 
 namespace {
@@ -168,6 +175,8 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
                    bp.tiles.size() * sizeof(TileDesc) + n_out * (sizeof(uint64_t) + sizeof(double));
     if ((e = cudaEventCreate(&db.ev_k0)) != cudaSuccess || (e = cudaEventCreate(&db.ev_k1)) != cudaSuccess)
         return cuda_fail(ctx, e, "cudaEventCreate");
+    if (!bp.cv.empty() && (e = cv_prepare(bp, st, &db.d_cv_eg, &db.d_cv_partner)) != cudaSuccess)
+        return cuda_fail(ctx, e, "control variate");
     return HEXO_OK;
 }
 
@@ -188,7 +197,7 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
         if ((e = launch_paths(db.f32, db.plan.shape, db.grid, db.smem, st, db.args)) != cudaSuccess) return e;
     if ((e = cudaEventRecordWithFlags(db.ev_k1, st, rec_flags)) != cudaSuccess) return e;
     if ((e = launch_finalize(db.args.acc, db.n_slots, db.args.acc_slot_stride, db.d_paths, db.d_disc, n_out,
-                             db.d_price, db.d_se, db.d_acc_sum, st)) != cudaSuccess)
+                             db.d_price, db.d_se, db.d_acc_sum, st, db.d_cv_eg, db.d_cv_partner)) != cudaSuccess)
         return e;
     if ((e = cudaMemcpyAsync(db.h_price, db.d_price, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_se, db.d_se, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
@@ -210,14 +219,16 @@ hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_re
                           uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans) {
     if (reqs == nullptr || n_reqs == 0) return ctx_fail(ctx, HEXO_ERR_INVALID, "no requests");
     plans.resize(n_reqs);
-    uint32_t out_base = 0;
+    uint32_t out_base = 0, cv_base = 0;
+    for (uint32_t r = 0; r < n_reqs; ++r) cv_base += reqs[r].n_opts;   // internal slots after all outputs
     for (uint32_t r = 0; r < n_reqs; ++r) {
         std::string err;
         hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, cfg, reqs[r].seed, path_lo,
                                  path_hi, plans[r], err);
         if (s != HEXO_OK) return ctx_fail(ctx, s, "request " + std::to_string(r) + ": " + err);
-        batch_add(bp, plans[r], out_base);
+        batch_add(bp, plans[r], out_base, cv_base);
         out_base += reqs[r].n_opts;
+        cv_base += 2u * plans[r].n_cv;
     }
     bp.shape = ctx_shape(ctx, cfg);
     batch_tiles(bp, plans);
@@ -434,6 +445,8 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
                                uint64_t *limbs_out) {
     if (!ctx || !p || !cfg || !limbs_out) return HEXO_ERR_INVALID;
     if (path_hi < path_lo) return ctx_fail(ctx, HEXO_ERR_INVALID, "path_hi < path_lo");
+    if (cfg->control_variate)
+        return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "the control variate is not supported by partial sums");
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     hexo_request r;
@@ -477,14 +490,16 @@ hexo_status hexo_plan_stats_get(const hexo_request *reqs, uint32_t n_reqs, const
     if (!reqs || n_reqs == 0 || !cfg || !out) return HEXO_ERR_INVALID;
     BatchPlan bp;
     std::vector<SetPlan> plans(n_reqs);
-    uint32_t base = 0, n_mats = 0, n_segs = 0;
+    uint32_t base = 0, n_mats = 0, n_segs = 0, cv_base = 0;
+    for (uint32_t r = 0; r < n_reqs; ++r) cv_base += reqs[r].n_opts;
     for (uint32_t r = 0; r < n_reqs; ++r) {
         std::string err;
         hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, *cfg, reqs[r].seed, 0,
                                  ~0ull, plans[r], err);
         if (s != HEXO_OK) return s;
-        batch_add(bp, plans[r], base);
+        batch_add(bp, plans[r], base, cv_base);
         base += reqs[r].n_opts;
+        cv_base += 2u * plans[r].n_cv;
         n_mats += (uint32_t)plans[r].mats.size();
         n_segs += (uint32_t)plans[r].segs.size();
     }

@@ -1,0 +1,283 @@
+// Geometric-average control variate (the future idea named in
+// HSimulation.h:51), its analytic half: E[(G - K)^+] under the Heston model
+// for every Asian option a batch prices with the control variate.
+//
+// Per path the kernels form L = (sum_k h_k (y_k + y_{k-1}) + (y_n - y_{n-1}) w) / T
+// on y = log(X / S0): the Asian contract's own weights (AsianContract.h:25-34,
+// its spot-difference term included) on the log-spot, and G = S0 exp(L).
+// L = sum_k c_k y_k is linear in the log-spot at the grid times, so its
+// characteristic function is a backward recursion of the Heston affine
+// solution over the grid steps: with Theta_k = z sum_{j >= k} c_j,
+//   E_{t_{k-1}}[exp(Theta_k (y_k - y_{k-1}) + b_k v_k)] = exp(A_k + b_{k-1} v_{k-1}),
+// and E[exp(z L)] = exp(sum_k A_k + b_0 v0).  The call follows from Lewis's
+// single integral (F = E[G], k = log(F / K)):
+//   E[(G - K)^+] = F - sqrt(F K) / pi  int_0^inf Re[e^{iuk} E[e^{(iu + 1/2)(L - log(F/S0))}]] / (u^2 + 1/4) du,
+// evaluated with Gauss-Legendre on [0, U] (256 nodes) and, through u = U / s,
+// on [U, inf) (128 nodes), U = 40 standard deviations of L.
+//
+// One thread per (maturity, node) runs the recursion in FP64 complex
+// arithmetic; one thread per option then sums the nodes.  Done once when a
+// batch is uploaded; the finaliser combines it with the path sums.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <algorithm>
+#include <map>
+#include <vector>
+#include "hexo_plan.h"
+#include "hexo_launch.h"
+
+namespace hexo {
+
+namespace {
+
+constexpr int kCvNodesNear = 256, kCvNodesTail = 128;
+constexpr int kCvNodes = kCvNodesNear + kCvNodesTail;
+constexpr double kCvRange = 40.0;
+
+struct CvMat {                     // one (set, maturity) with control-variate options
+    uint32_t step_begin, n_steps;  // its grid steps: (dt, c) in the step array
+    double U;                      // integration scale
+    double v0, kappa, theta, sigma, rho, mu, S0;
+};
+struct CvOpt {
+    uint32_t mat, out;             // CvMat index; output slot of the Asian option
+    double K;
+};
+
+struct cd { double x, y; };
+__device__ __forceinline__ cd cadd(cd a, cd b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ cd csub(cd a, cd b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ cd cmul(cd a, cd b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ cd cscale(cd a, double s) { return {a.x * s, a.y * s}; }
+__device__ __forceinline__ cd cdiv(cd a, cd b) {
+    const double d = b.x * b.x + b.y * b.y;
+    return {(a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d};
+}
+__device__ __forceinline__ cd cexp(cd a) {
+    double s, c;
+    sincos(a.y, &s, &c);
+    const double e = exp(a.x);
+    return {e * c, e * s};
+}
+__device__ __forceinline__ cd clog(cd a) { return {log(hypot(a.x, a.y)), atan2(a.y, a.x)}; }
+__device__ __forceinline__ cd csqrt(cd a) {   // principal branch
+    const double r = hypot(a.x, a.y);
+    if (r == 0.0) return {0.0, 0.0};
+    const double t = sqrt(0.5 * (r + fabs(a.x)));
+    return a.x >= 0.0 ? cd{t, a.y / (2.0 * t)} : cd{fabs(a.y) / (2.0 * t), copysign(t, a.y)};
+}
+
+// The Heston affine solution over tau with terminal exponent b:
+// E_t[exp(a (y_T - y_t) + b v_T)] = exp(A + B v_t) ("little trap" form).
+__device__ __forceinline__ void heston_affine(cd a, cd b, double tau, const CvMat &m, cd &A, cd &B) {
+    const double s2 = m.sigma * m.sigma;
+    const cd beta = {m.kappa - m.rho * m.sigma * a.x, -m.rho * m.sigma * a.y};
+    const cd am1 = {a.x - 1.0, a.y};
+    cd D = csqrt(csub(cmul(beta, beta), cscale(cmul(a, am1), s2)));
+    if (D.x < 0.0) D = {-D.x, -D.y};
+    const cd s2b = cscale(b, s2);
+    const cd g = cdiv(csub(csub(beta, D), s2b), csub(cadd(beta, D), s2b));
+    const cd e = cexp(cscale(D, -tau));
+    const cd ge = cmul(g, e);
+    const cd one_ge = {1.0 - ge.x, -ge.y};
+    B = cdiv(csub(csub(beta, D), cmul(cadd(beta, D), ge)), cscale(one_ge, s2));
+    const cd lg = clog(cdiv(one_ge, cd{1.0 - g.x, -g.y}));
+    const cd inner = csub(cscale(csub(beta, D), tau), cscale(lg, 2.0));
+    A = cadd(cscale(a, m.mu * tau), cscale(inner, m.kappa * m.theta / s2));
+}
+
+// phi[m * (kCvNodes + 1) + i] = E[exp(z L)], z = 1/2 + i U x_i for the nodes
+// and z = 1 (E[G] / S0) at i = kCvNodes.
+__global__ void cv_cf_kernel(const CvMat *__restrict__ mats, uint32_t n_mats, const double2 *__restrict__ steps,
+                             const double2 *__restrict__ nodes, double2 *__restrict__ phi) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_mats * (uint32_t)(kCvNodes + 1)) return;
+    const uint32_t mi = t / (kCvNodes + 1), i = t % (kCvNodes + 1);
+    const CvMat m = mats[mi];
+    const cd z = i == (uint32_t)kCvNodes ? cd{1.0, 0.0} : cd{0.5, m.U * nodes[i].x};
+    cd Asum = {0.0, 0.0}, b = {0.0, 0.0}, Th = {0.0, 0.0};
+    for (uint32_t k = m.n_steps; k-- > 0;) {
+        const double2 s = steps[m.step_begin + k];   // (dt, c)
+        Th = cadd(Th, cscale(z, s.y));
+        cd A, B;
+        heston_affine(Th, b, s.x, m, A, B);
+        Asum = cadd(Asum, A);
+        b = B;
+    }
+    const cd r = cexp(cadd(Asum, cscale(b, m.v0)));
+    phi[t] = make_double2(r.x, r.y);
+}
+
+// eg[out] = E[(G - K)^+] (undiscounted) for each control-variate option.
+__global__ void cv_price_kernel(const CvMat *__restrict__ mats, const CvOpt *__restrict__ opts, uint32_t n_opts,
+                                const double2 *__restrict__ nodes, const double2 *__restrict__ phi,
+                                double *__restrict__ eg) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_opts) return;
+    const CvOpt o = opts[q];
+    const CvMat m = mats[o.mat];
+    const double2 *ph = phi + (size_t)o.mat * (kCvNodes + 1);
+    const double F = m.S0 * ph[kCvNodes].x;
+    const double lf = log(F / m.S0), k = log(F / o.K);
+    double sum = 0.0;
+    for (int i = 0; i < kCvNodes; ++i) {
+        const double u = m.U * nodes[i].x, w = m.U * nodes[i].y;
+        const cd z = {0.5, u};
+        const cd psi = cmul(cd{ph[i].x, ph[i].y}, cexp(cscale(z, -lf)));
+        const cd ek = cexp(cd{0.0, u * k});
+        sum += w * cmul(ek, psi).x / (u * u + 0.25);
+    }
+    eg[o.out] = F - sqrt(F * o.K) / M_PI * sum;
+}
+
+// Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_N).
+void gauss_legendre(int N, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(N, 0.0);
+    w.assign(N, 0.0);
+    for (int i = 0; i < (N + 1) / 2; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (N + 0.5)), pp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int k = 1; k <= N; ++k) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * k - 1.0) * z * p2 - (k - 1.0) * p3) / k;
+            }
+            pp = N * (z * p1 - p2) / (z * z - 1.0);
+            const double dz = p1 / pp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[i] = -z;
+        x[N - 1 - i] = z;
+        w[i] = w[N - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+    }
+}
+
+// Unit-scale nodes: u = U x, weight U w, on [0, 1] and on [1, inf) via 1 / s.
+std::vector<double2> unit_nodes() {
+    std::vector<double> x1, w1, x2, w2;
+    gauss_legendre(kCvNodesNear, x1, w1);
+    gauss_legendre(kCvNodesTail, x2, w2);
+    std::vector<double2> n;
+    for (int i = 0; i < kCvNodesNear; ++i) n.push_back(make_double2(0.5 * (x1[i] + 1.0), 0.5 * w1[i]));
+    for (int i = 0; i < kCvNodesTail; ++i) {
+        const double s = 0.5 * (x2[i] + 1.0);
+        n.push_back(make_double2(1.0 / s, 0.5 * w2[i] / (s * s)));
+    }
+    return n;
+}
+
+// Grid steps (dt, c) of set s up to set-local maturity j: every step of the
+// segments up to the one that prices j; h_k is the segment's half width
+// after a non-pricing step and the next segment's after a pricing step.
+void cv_schedule(const BatchPlan &bp, uint32_t s, uint32_t j, std::vector<double2> &out, double &U) {
+    const SetDesc &sd = bp.sets[s];
+    std::vector<double> dts, h;
+    for (uint32_t q = 0; q < sd.seg_count; ++q) {
+        const SegDesc &g = bp.segs[sd.seg_begin + q];
+        const bool last = j >= g.mat_begin && j < g.mat_end;
+        for (uint32_t st = 1; st <= g.n_steps; ++st) {
+            dts.push_back(g.dt);
+            if (st < g.n_steps) h.push_back(g.hdt);
+            else if (!last) h.push_back(g.hdt_after);
+        }
+        if (last) break;
+    }
+    const MatDesc &md = bp.mats[sd.mat_begin + j];
+    const double T = md.T, w = md.tmtp / md.dt;
+    const size_t n = dts.size();
+    std::vector<double> c(n, 0.0);
+    for (size_t k = 1; k < n; ++k) {
+        c[k - 1] += h[k - 1];
+        if (k >= 2) c[k - 2] += h[k - 1];
+    }
+    if (n >= 2) c[n - 2] -= w;
+    c[n - 1] += w;
+    for (double &x : c) x /= T;
+    // the scale of L: its variance along the variance's mean path
+    const hexo_params &p = bp.set_params[s];
+    std::vector<double> Cws(n);
+    double Cw = 0.0, var = 0.0, t = 0.0;
+    for (size_t k = n; k-- > 0;) { Cw += c[k]; Cws[k] = Cw; }
+    for (size_t k = 0; k < n; ++k) {
+        const double Ev = p.theta + (p.v0 - p.theta) * std::exp(-p.kappa * t);
+        var += Cws[k] * Cws[k] * Ev * dts[k];
+        t += dts[k];
+    }
+    U = kCvRange / std::sqrt(std::max(var, 1e-12));
+    for (size_t k = 0; k < n; ++k) out.push_back(make_double2(dts[k], c[k]));
+}
+
+template <class T>
+cudaError_t upload(const std::vector<T> &v, T *&d, cudaStream_t st) {
+    cudaError_t e = cudaMalloc(&d, std::max<size_t>(1, v.size()) * sizeof(T));
+    if (e == cudaSuccess && !v.empty()) e = cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+    return e;
+}
+
+} // namespace
+
+// Computes E[(G - K)^+] of every control-variate option into eg (indexed by
+// output slot, NaN elsewhere) and the slot of its geometric sums into partner
+// (~0 elsewhere).  Both device arrays have n_out entries; allocated here.
+cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32_t **partner) {
+    *eg = nullptr;
+    *partner = nullptr;
+    std::vector<double> h_eg(bp.n_out, std::nan(""));
+    std::vector<uint32_t> h_partner(bp.n_out, ~0u);
+    std::vector<CvMat> mats;
+    std::vector<CvOpt> opts;
+    std::vector<double2> steps;
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> mat_of;
+    for (const BatchPlan::CvLeader &l : bp.cv) {
+        h_partner[l.leader] = l.gslot;
+        const auto key = std::make_pair(l.set, l.mat);
+        auto it = mat_of.find(key);
+        if (it == mat_of.end()) {
+            CvMat m{};
+            m.step_begin = (uint32_t)steps.size();
+            cv_schedule(bp, l.set, l.mat, steps, m.U);
+            m.n_steps = (uint32_t)steps.size() - m.step_begin;
+            const hexo_params &p = bp.set_params[l.set];
+            m.v0 = p.v0; m.kappa = p.kappa; m.theta = p.theta; m.sigma = p.sigma; m.rho = p.rho;
+            m.mu = p.r - p.q;
+            m.S0 = bp.sets[l.set].S0;
+            it = mat_of.emplace(key, (uint32_t)mats.size()).first;
+            mats.push_back(m);
+        }
+        opts.push_back(CvOpt{it->second, l.leader, l.strike});
+    }
+    const std::vector<double2> nodes = unit_nodes();
+    CvMat *d_mats = nullptr;
+    CvOpt *d_opts = nullptr;
+    double2 *d_steps = nullptr, *d_nodes = nullptr, *d_phi = nullptr;
+    cudaError_t e = upload(h_eg, *eg, st);
+    if (e == cudaSuccess) e = upload(h_partner, *partner, st);
+    if (e == cudaSuccess && !mats.empty()) {
+        if (e == cudaSuccess) e = upload(mats, d_mats, st);
+        if (e == cudaSuccess) e = upload(opts, d_opts, st);
+        if (e == cudaSuccess) e = upload(steps, d_steps, st);
+        if (e == cudaSuccess) e = upload(nodes, d_nodes, st);
+        if (e == cudaSuccess) e = cudaMalloc(&d_phi, mats.size() * (kCvNodes + 1) * sizeof(double2));
+        if (e == cudaSuccess) {
+            const uint32_t n_thr = (uint32_t)mats.size() * (kCvNodes + 1);
+            cv_cf_kernel<<<(n_thr + 127) / 128, 128, 0, st>>>(d_mats, (uint32_t)mats.size(), d_steps, d_nodes, d_phi);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            cv_price_kernel<<<((uint32_t)opts.size() + 127) / 128, 128, 0, st>>>(d_mats, d_opts, (uint32_t)opts.size(),
+                                                                                  d_nodes, d_phi, *eg);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the host vectors go out of scope
+    cudaFree(d_mats);
+    cudaFree(d_opts);
+    cudaFree(d_steps);
+    cudaFree(d_nodes);
+    cudaFree(d_phi);
+    return e;
+}
+
+} // namespace hexo

@@ -37,6 +37,54 @@ HEXO_HD double limbs_to_double(uint64_t l0, uint64_t l1, uint64_t l2) {
     return fadd(fmul(u64d(hi), 18446744073709551616.0), u64d(lo));
 }
 
+// An exact 128-bit sum converted to double.
+HEXO_HD double u128_to_double(unsigned __int128 s) {
+    const uint64_t hi = (uint64_t)(s >> 64), lo = (uint64_t)s;
+    return fadd(fmul(u64d(hi), 18446744073709551616.0), u64d(lo));
+}
+
+// Mean and (unbiased) variance of the values behind six limb sums; biased
+// sums (the control variate's signed differences) carry 2^63 per path in
+// their first sum.
+HEXO_HD void moments_limbs6(const uint64_t *l, uint64_t n_paths, bool biased, double *mean, double *var) {
+    const double n = u64d(n_paths);
+    const unsigned __int128 u = (unsigned __int128)l[0] + ((unsigned __int128)l[1] << 25) + ((unsigned __int128)l[2] << 50);
+    double s1;
+    if (biased) {
+        const __int128 v = (__int128)u - ((__int128)n_paths << 63);
+        s1 = v < 0 ? -u128_to_double((unsigned __int128)(-v)) : u128_to_double((unsigned __int128)v);
+    } else {
+        s1 = u128_to_double(u);
+    }
+    const double s2 = limbs_to_double(l[3], l[4], l[5]);
+    *mean = n_paths ? fdiv(fmul(s1, 0x1p-40), n) : 0.0;
+    const double m2 = n_paths ? fdiv(fmul(s2, 0x1p-24), n) : 0.0;
+    double v = 0.0;
+    if (n_paths > 1) v = fmul(fsub(m2, fmul(*mean, *mean)), fdiv(n, fsub(n, 1.0)));
+    *var = v > 0.0 ? v : 0.0;
+}
+
+// The control-variate estimate of an Asian option from the sums of
+// a = (A - K)^+, g = (G - K)^+ and d = a - g over the same paths:
+// Cov(a, g) = (Var a + Var g - Var d) / 2, beta = Cov / Var g, price
+// disc (mean a - beta (mean g - eg)), standard error that of a - beta g.
+HEXO_HD void finalize_cv(const uint64_t *la, const uint64_t *lg, const uint64_t *ld, uint64_t n_paths, double disc,
+                         double eg, double *price, double *se) {
+    double ma, va, mg, vg, md, vd;
+    moments_limbs6(la, n_paths, false, &ma, &va);
+    moments_limbs6(lg, n_paths, false, &mg, &vg);
+    moments_limbs6(ld, n_paths, true, &md, &vd);
+    double mean = ma, var = va;
+    if (vg > 0.0) {
+        const double cov = fmul(fsub(fadd(va, vg), vd), 0.5);
+        mean = fsub(ma, fmul(fdiv(cov, vg), fsub(mg, eg)));
+        var = fsub(va, fdiv(fmul(cov, cov), vg));
+        if (!(var > 0.0)) var = 0.0;
+    }
+    *price = fmul(disc, mean);
+    *se = n_paths ? fmul(disc, fsqr(fdiv(var, u64d(n_paths)))) : 0.0;
+}
+
 HEXO_HD void finalize_limbs6(const uint64_t *l, uint64_t n_paths, double disc, double *price, double *se) {
     const double n = u64d(n_paths);
     const double s1 = limbs_to_double(l[0], l[1], l[2]);

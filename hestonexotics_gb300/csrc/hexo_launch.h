@@ -17,11 +17,12 @@ inline size_t paths_smem_bytes(uint32_t block, uint32_t ppt) {
     return (rings + 15) / 16 * 16 + (size_t)(block / 32) * 64u * kLimbs * sizeof(uint32_t) + 128u * 16u;
 }
 
-// nullptr when (ppt, unroll) is not instantiated.
-const void *paths_kernel_ptr_f64(uint32_t ppt, uint32_t unroll);
-const void *paths_kernel_ptr_f32(uint32_t ppt, uint32_t unroll);
-inline const void *paths_kernel_ptr(bool f32, uint32_t ppt, uint32_t unroll) {
-    return f32 ? paths_kernel_ptr_f32(ppt, unroll) : paths_kernel_ptr_f64(ppt, unroll);
+// nullptr when (ppt, unroll) is not instantiated; the control-variate
+// kernels (cv) exist for one path per thread and no unrolling.
+const void *paths_kernel_ptr_f64(uint32_t ppt, uint32_t unroll, bool cv);
+const void *paths_kernel_ptr_f32(uint32_t ppt, uint32_t unroll, bool cv);
+inline const void *paths_kernel_ptr(bool f32, uint32_t ppt, uint32_t unroll, bool cv = false) {
+    return f32 ? paths_kernel_ptr_f32(ppt, unroll, cv) : paths_kernel_ptr_f64(ppt, unroll, cv);
 }
 cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t smem, cudaStream_t st,
                          const KernelArgs &a);
@@ -30,7 +31,12 @@ cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t 
 // null, receives the totals) and writes price and standard error per slot.
 cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
                             const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
-                            unsigned long long *acc_sum, cudaStream_t st);
+                            unsigned long long *acc_sum, cudaStream_t st, const double *cv_eg = nullptr,
+                            const uint32_t *cv_partner = nullptr);
+// The geometric control variate's analytic part for a planned batch:
+// E[(G - K)^+] per control-variate option into *eg and its geometric-sum slot
+// into *partner (device arrays of n_out entries, allocated here).
+cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32_t **partner);
 
 // Debug kernels.
 cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st);

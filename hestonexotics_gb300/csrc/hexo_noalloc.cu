@@ -136,6 +136,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     if (!pp || !opts || !cfg || !price_out) return HEXO_ERR_INVALID;
     if (n_opts == 0) return HEXO_ERR_INVALID;
     if (n_opts > kNaMaxOptions) return HEXO_ERR_TOO_LARGE;
+    if (cfg->control_variate) return HEXO_ERR_UNSUPPORTED;
     const hexo_params p = *pp;
     const double pv[7] = {p.v0, p.theta, p.rho, p.kappa, p.sigma, p.r, p.q};
     for (double x : pv)

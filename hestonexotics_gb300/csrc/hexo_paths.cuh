@@ -177,25 +177,46 @@ constexpr uint32_t kWindow = 64;
 // option oi of this warp's paths into the warp's window entry wslot: exact
 // limbs per path, one warp sum per limb (redux.sync), stored by lane 0.  A
 // warp whose payoffs are all 0 leaves its (cleared) window entry as it is.
-template <bool kF32, int PPT>
+// With the control variate (kCV), kind 2 folds the geometric-average call
+// (G - K)^+ and kind 3 the signed difference (A - K)^+ - (G - K)^+, whose
+// biased limbs are written for every counted path.
+template <bool kF32, int PPT, bool kCV>
 __device__ __forceinline__ void fold_option(const KernelArgs &a, const SetDesc &S, uint32_t oi, uint32_t *wslot,
                                             uint32_t lane, const bool (&active)[PPT], const uint64_t (&kpath)[PPT],
                                             const typename Real<kF32>::T (&asian)[PPT],
-                                            const typename Real<kF32>::T (&euro)[PPT]) {
+                                            const typename Real<kF32>::T (&euro)[PPT],
+                                            const typename Real<kF32>::T (&geo)[PPT]) {
     const OptDesc &O = a.opts[S.opt_begin + oi];
     uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
     bool ok = true, any = false;
+    const uint32_t kind = O.kind;
 #pragma unroll
     for (int p = 0; p < PPT; ++p) {
         if (active[p] && kpath[p] < O.n_paths) {
             if constexpr (kF32) {
-                const float pay = fmaxf(0.0f, __fsub_rn(O.kind == 0 ? asian[p] : euro[p], O.f_strike));
-                any |= pay != 0.0f;
-                ok &= dev::limbs_add_f32(pay, l);
+                const float K = O.f_strike;
+                if (kCV && kind == 3u) {
+                    const float d = __fsub_rn(fmaxf(0.0f, __fsub_rn(asian[p], K)), fmaxf(0.0f, __fsub_rn(geo[p], K)));
+                    any = true;   // every counted path adds its 2^63 bias, zero or not
+                    ok &= dev::limbs_add_signed_f32(d, l);
+                } else {
+                    const float f = kind == 0u ? asian[p] : (kCV && kind == 2u) ? geo[p] : euro[p];
+                    const float pay = fmaxf(0.0f, __fsub_rn(f, K));
+                    any |= pay != 0.0f;
+                    ok &= dev::limbs_add_f32(pay, l);
+                }
             } else {
-                const double pay = fmax(0.0, __dsub_rn(O.kind == 0 ? asian[p] : euro[p], O.strike));
-                any |= pay != 0.0;
-                ok &= dev::limbs_add_f64(pay, l);
+                const double K = O.strike;
+                if (kCV && kind == 3u) {
+                    const double d = __dsub_rn(fmax(0.0, __dsub_rn(asian[p], K)), fmax(0.0, __dsub_rn(geo[p], K)));
+                    any = true;   // every counted path adds its 2^63 bias, zero or not
+                    ok &= dev::limbs_add_signed_f64(d, l);
+                } else {
+                    const double f = kind == 0u ? asian[p] : (kCV && kind == 2u) ? geo[p] : euro[p];
+                    const double pay = fmax(0.0, __dsub_rn(f, K));
+                    any |= pay != 0.0;
+                    ok &= dev::limbs_add_f64(pay, l);
+                }
             }
         }
     }
@@ -213,7 +234,7 @@ __device__ __forceinline__ void fold_option(const KernelArgs &a, const SetDesc &
     }
 }
 
-template <bool kF32, int PPT, int UNROLL>
+template <bool kF32, int PPT, int UNROLL, bool kCV = false>
 __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
     typedef typename Real<kF32>::T R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -279,6 +300,9 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         dev::Shishua g[PPT];
         dev::RngLane c[PPT];
         PathVars<kF32> pv[PPT];
+        // control variate: y = log(X / S0) now and one step back, and the
+        // Asian contract's trapezoid sum on y (the geometric average's log)
+        R yc[PPT], yp[PPT], accg[PPT];
         uint64_t kpath[PPT];
         bool active[PPT];
 #pragma unroll
@@ -292,6 +316,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             pv[p].X = kF32 ? (R)S.f_S0 : (R)S.S0;
             pv[p].Xp = pv[p].X;
             pv[p].acc = (R)0;
+            yc[p] = yp[p] = accg[p] = (R)0;
         }
 
         for (uint32_t si = 0; si < td.seg_count; ++si) {
@@ -308,12 +333,20 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                     if constexpr (kF32) quad = qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
                     else quad = qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
                     n_quad += (active[p] && quad) ? 1u : 0u;
-                    if (st < sg.n_steps) pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
+                    if constexpr (kCV) {
+                        yp[p] = yc[p];   // FP32: the exponent of X / S0 that qe_step used
+                        if constexpr (kF32) yc[p] = __fmaf_rn(rf, pv[p].v, pv[p].lx);
+                        else yc[p] = __dsub_rn(pv[p].lx, S.logS0);
+                    }
+                    if (st < sg.n_steps) {
+                        pv[p].acc = fma_r(hdt, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
+                        if constexpr (kCV) accg[p] = fma_r(hdt, add_r(yc[p], yp[p]), accg[p]);
+                    }
                 }
             }
             for (uint32_t mj = sg.mat_begin; mj < sg.mat_end; ++mj) {
                 const MatDesc M = a.mats[S.mat_begin + mj];
-                R asian[PPT], euro[PPT];
+                R asian[PPT], euro[PPT], geo[PPT];
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
                     R interp;
@@ -325,6 +358,18 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                         asian[p] = __ddiv_rn(__dadd_rn(pv[p].acc, interp), M.T);
                     }
                     euro[p] = add_r(pv[p].Xp, interp);                     // VanillaContract.h:28-29
+                    geo[p] = (R)0;
+                    if constexpr (kCV) {   // G = S0 exp(L), L the Asian weights on y
+                        if constexpr (kF32) {
+                            const float L = __fmul_rn(__fadd_rn(accg[p], __fmul_rn(__fsub_rn(yc[p], yp[p]), M.f_w)),
+                                                      M.f_invT);
+                            geo[p] = __fmul_rn(S0f, expf(L));
+                        } else {
+                            const double L = __ddiv_rn(
+                                __dadd_rn(accg[p], __ddiv_rn(__dmul_rn(__dsub_rn(yc[p], yp[p]), M.tmtp), M.dt)), M.T);
+                            geo[p] = __dmul_rn(S.S0, exp(L));
+                        }
+                    }
                     if (a.dbg_asian != nullptr && active[p]) {
                         const size_t at = (size_t)(kpath[p] - a.dbg_lo) * a.dbg_mats + mj;
                         a.dbg_asian[at] = (double)asian[p];
@@ -337,12 +382,16 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                         flush(S, win_base);
                         win_base = oi - oi % kWindow;
                     }
-                    fold_option<kF32, PPT>(a, S, oi, wwin + (oi - win_base) * kLimbs, lane, active, kpath, asian, euro);
+                    fold_option<kF32, PPT, kCV>(a, S, oi, wwin + (oi - win_base) * kLimbs, lane, active, kpath, asian,
+                                                euro, geo);
                 }
             }
             const R hda = kF32 ? (R)sg.f_hdt_after : (R)sg.hdt_after;
 #pragma unroll
-            for (int p = 0; p < PPT; ++p) pv[p].acc = fma_r(hda, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
+            for (int p = 0; p < PPT; ++p) {
+                pv[p].acc = fma_r(hda, add_r(pv[p].X, pv[p].Xp), pv[p].acc);
+                if constexpr (kCV) accg[p] = fma_r(hda, add_r(yc[p], yp[p]), accg[p]);
+            }
         }
         flush(S, win_base);
         if (a.quad_steps != nullptr) {   // branch mix of the launch, one atomic per warp and tile

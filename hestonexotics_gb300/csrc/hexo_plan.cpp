@@ -36,6 +36,7 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
     if (cfg.step_mode > 1u) { err = "unknown step mode"; return HEXO_ERR_INVALID; }
     if (cfg.step_mode == HEXO_STEP_REFERENCE && cfg.steps == 0) { err = "steps must be positive"; return HEXO_ERR_INVALID; }
     if (cfg.precision > 1u) { err = "unknown precision"; return HEXO_ERR_INVALID; }
+    if (cfg.control_variate > 1u) { err = "unknown control variate"; return HEXO_ERR_INVALID; }
 
     // Group options by distinct maturity, ascending; stable within a maturity.
     std::vector<uint32_t> idx(n_opts);
@@ -74,9 +75,23 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
         od.out_index = i;
         out.opts.push_back(od);
         out.opt_disc.push_back(std::exp(-p.r * opts[i].T));
+        if (cfg.control_variate && od.kind == HEXO_ASIAN_CALL) {
+            // the geometric call and the difference follow their Asian option, in
+            // request-local slots n_opts + 2 c and n_opts + 2 c + 1
+            for (uint32_t x = 0; x < 2; ++x) {
+                OptDesc cv = od;
+                cv.kind = 2u + x;
+                cv.out_index = n_opts + 2u * out.n_cv + x;
+                out.opts.push_back(cv);
+                out.opt_disc.push_back(out.opt_disc.back());
+            }
+            ++out.n_cv;
+        }
         out.mats.back().opt_end = (uint32_t)out.opts.size();
         out.mat_paths.back() = std::max(out.mat_paths.back(), od.n_paths);
     }
+    out.n_user = n_opts;
+    out.params = p;
     const size_t m = T.size();
 
     // Walk the reference's time grid once (HSimulation.tpp:29-46,
@@ -192,7 +207,10 @@ void plan_work(const SetPlan &sp, uint64_t &nominal, uint64_t &executed, uint32_
     }
 }
 
-void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base) {
+void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_base) {
+    // request-local slots: the user's options, then the control variate's
+    // internal pairs, which go to the batch's internal range at cv_base
+    auto global = [&](uint32_t local) { return local < sp.n_user ? out_base + local : cv_base + (local - sp.n_user); };
     SetDesc sd = sp.set;
     sd.seg_begin = (uint32_t)b.segs.size();
     sd.mat_begin = (uint32_t)b.mats.size();
@@ -202,23 +220,30 @@ void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base) {
     b.mats.insert(b.mats.end(), sp.mats.begin(), sp.mats.end());
     for (size_t i = 0; i < sp.opts.size(); ++i) {
         OptDesc od = sp.opts[i];
-        od.out_index = out_base + sp.opts[i].out_index;
+        od.out_index = global(sp.opts[i].out_index);
         b.opts.push_back(od);
     }
-    const uint32_t n_out_end = out_base + (uint32_t)sp.opts.size();
+    uint32_t n_out_end = out_base + sp.n_user;
+    if (sp.n_cv) n_out_end = std::max(n_out_end, cv_base + 2u * sp.n_cv);
     if (b.n_out < n_out_end) {
         b.n_out = n_out_end;
         b.opt_paths.resize(n_out_end, 0);
         b.opt_disc.resize(n_out_end, 1.0);
     }
     for (size_t i = 0; i < sp.opts.size(); ++i) {
-        const uint32_t o = out_base + sp.opts[i].out_index;
+        const uint32_t o = global(sp.opts[i].out_index);
         // paths that price this option within the plan's range
         const uint64_t hi = std::min<uint64_t>(sp.opts[i].n_paths, sp.path_hi);
         b.opt_paths[o] = hi > sp.path_lo ? hi - sp.path_lo : 0;
         b.opt_disc[o] = sp.opt_disc[i];
     }
     b.max_mats = std::max<uint32_t>(b.max_mats, (uint32_t)sp.mats.size());
+    b.set_params.push_back(sp.params);
+    for (uint32_t j = 0; j < (uint32_t)sp.mats.size(); ++j)
+        for (uint32_t i = sp.mats[j].opt_begin; i < sp.mats[j].opt_end; ++i)
+            if (sp.opts[i].kind == 2u)   // the geometric slot, right after its Asian option
+                b.cv.push_back(BatchPlan::CvLeader{global(sp.opts[i - 1].out_index), global(sp.opts[i].out_index),
+                                                   (uint32_t)b.sets.size() - 1u, j, sp.opts[i].strike});
 }
 
 void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans) {

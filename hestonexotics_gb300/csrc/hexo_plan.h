@@ -11,6 +11,7 @@ namespace hexo {
 
 struct LaunchShape {
     uint32_t block = 256, ppt = 1, unroll = 1;
+    bool cv = false;   // the geometric control variate's kernel (one path per thread, no unroll)
     uint32_t paths_per_tile() const { return block * ppt; }
 };
 
@@ -28,6 +29,9 @@ struct SetPlan {
     std::vector<uint32_t> seg_of_mat;   // segment whose last step prices maturity j
     std::vector<uint64_t> steps_to_mat; // executed steps up to and including the pricing step of j
     uint64_t path_lo = 0, path_hi = 0;  // simulated path range
+    uint32_t n_user = 0;                // the request's options (request-local slots [0, n_user))
+    uint32_t n_cv = 0;                  // Asian options with the control variate (2 internal slots each)
+    hexo_params params{};
 };
 
 // Validates and plans one request.  Returns HEXO_OK or an error with a message.
@@ -51,14 +55,22 @@ struct BatchPlan {
     std::vector<TileDesc> tiles;
     std::vector<uint64_t> opt_paths;    // per output slot: paths that price it
     std::vector<double> opt_disc;       // per output slot: exp(-r T)
-    uint32_t n_out = 0;                 // output slots (sum of request option counts)
+    uint32_t n_out = 0;                 // output slots: the requests' options, then the control variate's
+    std::vector<hexo_params> set_params;
+    struct CvLeader {                   // an Asian option priced with the geometric control variate
+        uint32_t leader, gslot;         // its output slot; the geometric call's (the difference's is gslot + 1)
+        uint32_t set, mat;              // set and set-local maturity
+        double strike;
+    };
+    std::vector<CvLeader> cv;
     uint32_t max_mats = 0;
     uint64_t nominal_path_steps = 0, executed_path_steps = 0, n_paths = 0;
     LaunchShape shape;
 };
 
-// Appends a planned set whose outputs start at out_base.
-void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base);
+// Appends a planned set whose outputs start at out_base; its control-variate
+// slots (if any) start at cv_base, after every request's outputs.
+void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_base = 0);
 // Builds the tile list for the batch's launch shape, longest tiles first.
 void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans);
 

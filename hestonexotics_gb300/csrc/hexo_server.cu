@@ -205,11 +205,13 @@ bool launch_next(hexo_server *s, std::unique_lock<std::mutex> &lk) {
     BatchPlan bp;
     std::vector<SetPlan> plans;
     plans.reserve(batch.size());
-    uint32_t base = 0;
+    uint32_t base = 0, cv_base = 0;
+    for (SrvReq *r : batch) cv_base += r->req.n_opts;   // control-variate slots after all outputs
     for (SrvReq *r : batch) {
         plans.push_back(r->plan);
-        batch_add(bp, plans.back(), base);
+        batch_add(bp, plans.back(), base, cv_base);
         base += r->req.n_opts;
+        cv_base += 2u * r->plan.n_cv;
     }
     bp.shape = ctx_shape(s->ctx, s->opts.cfg);
     batch_tiles(bp, plans);

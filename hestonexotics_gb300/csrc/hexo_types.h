@@ -57,7 +57,8 @@ struct MatDesc {
 struct OptDesc {
     double strike;
     float f_strike;
-    uint32_t kind;       // 0 Asian, 1 European
+    uint32_t kind;       // 0 Asian, 1 European; with the control variate: 2 geometric-average call
+                         // (G - K)^+, 3 the signed difference (A - K)^+ - (G - K)^+
     uint64_t n_paths;    // paths k < n_paths price this option
     uint32_t out_index;  // position in the batch's result arrays
     uint32_t pad;

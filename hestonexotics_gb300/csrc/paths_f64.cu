@@ -4,7 +4,8 @@
 
 namespace hexo {
 
-const void *paths_kernel_ptr_f64(uint32_t ppt, uint32_t unroll) {
+const void *paths_kernel_ptr_f64(uint32_t ppt, uint32_t unroll, bool cv) {
+    if (cv) return ppt == 1 && unroll == 1 ? (const void *)paths_kernel<false, 1, 1, true> : nullptr;
     switch (ppt * 10u + unroll) {
     case 11: return (const void *)paths_kernel<false, 1, 1>;
     case 12: return (const void *)paths_kernel<false, 1, 2>;

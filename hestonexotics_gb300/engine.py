@@ -52,10 +52,12 @@ class Config:
     block: int = 0
     paths_per_thread: int = 0
     unroll: int = 0
+    control_variate: int = 0   # 1: Asian options with the geometric-average control variate
 
     def c(self) -> L.hexo_mc_cfg:
         return L.hexo_mc_cfg(self.n_paths, self.step_mode, self.steps, self.steps_per_year, self.seed & 0xFFFFFFFF,
-                             self.rng_block_words, self.precision, self.block, self.paths_per_thread, self.unroll)
+                             self.rng_block_words, self.precision, self.block, self.paths_per_thread, self.unroll,
+                             self.control_variate, 0)
 
 
 @dataclass

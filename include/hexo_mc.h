@@ -40,8 +40,9 @@ extern "C" {
 
 /* Raised whenever a struct's layout or a function's signature changes.
  * 2: hexo_batch_info.quad_steps; hexo_debug_pipe_peaks fills five rates;
- *    hexo_debug_payoff_limbs. */
-#define HEXO_ABI_VERSION 2u
+ *    hexo_debug_payoff_limbs.
+ * 3: hexo_mc_cfg.control_variate. */
+#define HEXO_ABI_VERSION 3u
 
 typedef enum hexo_status {
     HEXO_OK = 0,
@@ -129,6 +130,13 @@ typedef struct hexo_mc_cfg {
     uint32_t block;           /* launch shape override: threads per CTA, 0 = tuned/default */
     uint32_t paths_per_thread;/* 0 = tuned/default */
     uint32_t unroll;          /* 0 = tuned/default */
+    uint32_t control_variate; /* 0: the reference's estimator (default).  1: Asian options are priced
+                                 with the geometric-average control variate (the future idea of
+                                 HSimulation.h:51): the same weights on log X give G, E[(G - K)^+]
+                                 comes from the Heston characteristic function, and beta is
+                                 estimated from the paths; Europeans unchanged.  Not with
+                                 hexo_price_partial or hexo_price_noalloc. */
+    uint32_t reserved;
 } hexo_mc_cfg;
 
 /* Fills cfg with the defaults: 65,536 paths, REFERENCE stepping with 252

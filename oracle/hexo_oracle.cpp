@@ -42,6 +42,7 @@
 #include <vector>
 #include <algorithm>
 #include <numeric>
+#include <complex>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -153,13 +154,18 @@ struct Problem {
 template <class Visit>
 inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&visit, uint64_t *counts = nullptr) {
     PathState st{pr.S0, pr.S0, pr.p.v0, pr.p.v0, 0., 0., std::log(pr.S0)};
+    const double logS0 = st.logX;
     const size_t m = pr.T.size();
     size_t j = 0;
     uint64_t n_quad = 0, n_steps = 0;   // optional branch counts (counts[0], counts[1])
     double dt = pr.T[0] / pr.steps[0];  // update_earliest, AsianContract.h:35-38
     double acc = 0.;                    // reset, AsianContract.h:39-42
+    // the control variate's geometric counterpart of the Asian average: the
+    // same weights on y = log(X / S0) instead of X
+    double yc = 0., yp = 0., accg = 0.;
     n_quad += qe_step(st, pr.p, dt, rng);   // ++(heston_sde = initial_state), tpp:35
     ++n_steps;
+    yp = yc; yc = st.logX - logS0;
     for (;;) {
         bool more = true;
         while (j < m && st.t >= pr.T[j]) {                              // tpp:36
@@ -167,7 +173,8 @@ inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&v
             double interp = (st.Xc - st.Xp) * (T - st.tp) / dt;
             double asian = (acc + interp) / T;                          // AsianContract.h:29-34
             double euro = st.Xp + (st.Xc - st.Xp) * (T - st.tp) / dt;   // VanillaContract.h:28-31
-            more = visit(j, asian, euro);
+            double geo = pr.S0 * std::exp((accg + (yc - yp) * (T - st.tp) / dt) / T);
+            more = visit(j, asian, euro, geo);
             ++j;
             if (j < m) dt = pr.T[j] / pr.steps[j];                      // tpp:41-42
             if (!more) break;
@@ -178,8 +185,10 @@ inline void run_path(const Problem &pr, OracleRNG &rng, bool trailing, Visit &&v
             return;
         }
         acc += dt * .5 * (st.Xc + st.Xp);                               // AsianContract.h:25-28
+        accg += dt * .5 * (yc + yp);
         n_quad += qe_step(st, pr.p, dt, rng);
         ++n_steps;
+        yp = yc; yc = st.logX - logS0;
     }
 }
 
@@ -240,6 +249,152 @@ int build_problem(Problem &pr, const double *params7, double S0, uint32_t n_opts
     }
     return 0;
 }
+
+
+/* ---------------------------------------------------------------------
+ * Geometric-average control variate (the future idea of HSimulation.h:51).
+ *
+ * Per path, L = (sum_k h_k (y_k + y_{k-1}) + (y_n - y_{n-1}) w) / T on
+ * y = log(X / S0): the Asian contract's weights (AsianContract.h:25-34,
+ * the spot-difference term included) on the log-spot, and G = S0 exp(L).
+ * E[(G - K)^+] under the Heston model itself (continuous time, the same
+ * time grid) comes from the characteristic function of L, a backward
+ * recursion of the affine solution over the grid steps, and Lewis's single
+ * integral; the estimator is mean((A - K)^+ - (G - K)^+) + E[(G - K)^+].
+ * ------------------------------------------------------------------- */
+
+/* The grid steps up to maturity jt and the weights c_k of y_1..y_n in L,
+ * walking the time grid exactly as run_path does. */
+void cv_schedule(const Problem &pr, size_t jt, std::vector<double> &dts, std::vector<double> &c) {
+    const size_t m = pr.T.size();
+    double t = 0., tp = 0., dt = pr.T[0] / pr.steps[0];
+    size_t j = 0;
+    std::vector<double> h;   // h[k-1] weighs y_k + y_{k-1}
+    dts.clear();
+    tp = t; t += dt; dts.push_back(dt);
+    for (;;) {
+        while (j < m && t >= pr.T[j]) {
+            if (j == jt) {
+                const double T = pr.T[j], w = (T - tp) / dt;
+                const size_t n = dts.size();
+                c.assign(n, 0.);
+                for (size_t k = 1; k < n; ++k) {
+                    c[k - 1] += h[k - 1];
+                    if (k >= 2) c[k - 2] += h[k - 1];
+                }
+                if (n >= 2) c[n - 2] -= w;
+                c[n - 1] += w;
+                for (double &x : c) x /= T;
+                return;
+            }
+            ++j;
+            if (j < m) dt = pr.T[j] / pr.steps[j];
+        }
+        h.push_back(dt * .5);
+        tp = t; t += dt; dts.push_back(dt);
+    }
+}
+
+typedef std::complex<double> cplx;
+
+/* E_t[exp(a (y_T - y_t) + b v_T)] = exp(A + B v_t) over tau = T - t:
+ * the Heston affine solution with terminal b (the "little trap" form). */
+inline void heston_affine(cplx a, cplx b, double tau, const Params &p, cplx &A, cplx &B) {
+    const double s2 = p.sigma * p.sigma, mu = p.r - p.q;
+    const cplx beta = p.kappa - p.rho * p.sigma * a;
+    cplx D = std::sqrt(beta * beta - s2 * a * (a - 1.));
+    if (D.real() < 0.) D = -D;
+    const cplx g = (beta - D - s2 * b) / (beta + D - s2 * b);
+    const cplx e = std::exp(-D * tau);
+    B = ((beta - D) - (beta + D) * g * e) / (s2 * (1. - g * e));
+    A = a * mu * tau + p.kappa * p.theta / s2 * ((beta - D) * tau - 2. * std::log((1. - g * e) / (1. - g)));
+}
+
+/* E[exp(z L)] for complex z. */
+inline cplx cf_L(cplx z, const std::vector<double> &dts, const std::vector<double> &c, const Params &p) {
+    cplx Asum = 0., b = 0., Th = 0.;
+    for (size_t k = dts.size(); k-- > 0;) {
+        Th += z * c[k];                        // weight of the increment of step k+1
+        cplx A, B;
+        heston_affine(Th, b, dts[k], p, A, B);
+        Asum += A;
+        b = B;
+    }
+    return std::exp(Asum + b * p.v0);
+}
+
+/* Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_N). */
+void gauss_legendre(int N, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(N, 0.); w.assign(N, 0.);
+    for (int i = 0; i < (N + 1) / 2; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (N + 0.5)), pp = 0.;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1., p2 = 0.;
+            for (int k = 1; k <= N; ++k) { const double p3 = p2; p2 = p1; p1 = ((2. * k - 1.) * z * p2 - (k - 1.) * p3) / k; }
+            pp = N * (z * p1 - p2) / (z * z - 1.);
+            const double dz = p1 / pp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[i] = -z; x[N - 1 - i] = z;
+        w[i] = w[N - 1 - i] = 2. / ((1. - z * z) * pp * pp);
+    }
+}
+
+constexpr int kCvNodesNear = 256, kCvNodesTail = 128;   // [0, U] and [U, inf) by u = U / s
+constexpr double kCvRange = 40.;                        // U = 40 standard deviations of L
+
+/* E[G] and E[(G - K_i)^+] for the strikes of one maturity (undiscounted). */
+void cv_geo_calls(const Params &p, double S0, const std::vector<double> &dts, const std::vector<double> &c,
+                  const double *K, size_t nk, double *out, double *F_out) {
+    const double F = S0 * cf_L(1., dts, c, p).real();
+    // the scale of L from its variance with the variance's mean path
+    double var = 0., t = 0., Cw = 0.;
+    std::vector<double> Cws(dts.size());
+    for (size_t k = dts.size(); k-- > 0;) { Cw += c[k]; Cws[k] = Cw; }
+    for (size_t k = 0; k < dts.size(); ++k) {
+        const double Ev = p.theta + (p.v0 - p.theta) * std::exp(-p.kappa * t);
+        var += Cws[k] * Cws[k] * Ev * dts[k];
+        t += dts[k];
+    }
+    const double U = kCvRange / std::sqrt(std::max(var, 1e-12));
+    std::vector<double> x1, w1, x2, w2;
+    gauss_legendre(kCvNodesNear, x1, w1);
+    gauss_legendre(kCvNodesTail, x2, w2);
+    std::vector<double> u, w;
+    for (int i = 0; i < kCvNodesNear; ++i) { u.push_back(.5 * U * (x1[i] + 1.)); w.push_back(.5 * U * w1[i]); }
+    for (int i = 0; i < kCvNodesTail; ++i) { const double s = .5 * (x2[i] + 1.); u.push_back(U / s); w.push_back(.5 * w2[i] * U / (s * s)); }
+    const double lf = std::log(F / S0);
+    std::vector<cplx> psi(u.size());
+    for (size_t i = 0; i < u.size(); ++i) {
+        const cplx z(.5, u[i]);
+        psi[i] = cf_L(z, dts, c, p) * std::exp(-z * lf);
+    }
+    for (size_t q = 0; q < nk; ++q) {
+        const double k = std::log(F / K[q]);
+        double sum = 0.;
+        for (size_t i = 0; i < u.size(); ++i)
+            sum += w[i] * (std::exp(cplx(0., u[i] * k)) * psi[i]).real() / (u[i] * u[i] + .25);
+        out[q] = F - std::sqrt(F * K[q]) / M_PI * sum;
+    }
+    if (F_out) *F_out = F;
+}
+
+/* Signed fixed-point sums of the control variate's differences: q + 2^63
+ * (q = round(d 2^40)) and q2 = round(d^2 2^24), three 25-bit limbs each. */
+struct SignedSums {
+    std::vector<uint64_t> l;
+    explicit SignedSums(size_t n) : l(6 * n, 0) {}
+    void add(uint32_t o, double d) {
+        const __int128 q = (__int128)std::nearbyint(d * 0x1p40);
+        const unsigned __int128 qu = (unsigned __int128)(q + ((__int128)1 << 63));
+        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(d * d * 0x1p24);
+        const uint64_t M = (1ull << 25) - 1;
+        uint64_t *dd = &l[6 * (size_t)o];
+        dd[0] += (uint64_t)(qu & M); dd[1] += (uint64_t)((qu >> 25) & M); dd[2] += (uint64_t)(qu >> 50);
+        dd[3] += (uint64_t)(q2 & M); dd[4] += (uint64_t)((q2 >> 25) & M); dd[5] += (uint64_t)(q2 >> 50);
+    }
+};
 
 } // namespace
 
@@ -312,7 +467,7 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
         for (size_t j = 0; j < pr.T.size(); ++j)
             if (mat_paths[j] > (uint64_t)k) last = j;
         OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
-        run_path(pr, rng, false, [&](size_t j, double asian, double euro) {
+        run_path(pr, rng, false, [&](size_t j, double asian, double euro, double) {
             for (uint32_t o : pr.opts[j])
                 if ((uint64_t)k < n_paths[o]) acc.add(o, payoff_of(pr, o, asian, euro));
             return j < last;
@@ -369,7 +524,7 @@ int oracle_branch_counts(const double *params7, double S0, uint32_t n_opts, cons
         for (size_t j = 0; j < pr.T.size(); ++j)
             if (mat_paths[j] > (uint64_t)k) last = j;
         OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
-        run_path(pr, rng, false, [&](size_t j, double, double) { return j < last; }, c);
+        run_path(pr, rng, false, [&](size_t j, double, double, double) { return j < last; }, c);
     }
     counts[0] = counts[1] = 0;
     for (int t = 0; t < nt; ++t) { counts[0] += part[2 * (size_t)t]; counts[1] += part[2 * (size_t)t + 1]; }
@@ -405,7 +560,7 @@ int oracle_path_finals(const double *params7, double S0, uint32_t n_opts, const 
         }
         if (!any) continue;
         OracleRNG rng(block_words, static_cast<uint32_t>(seed + k));
-        run_path(pr, rng, false, [&](size_t j, double asian, double euro) {
+        run_path(pr, rng, false, [&](size_t j, double asian, double euro, double) {
             asian_out[(k - path_lo) * m + j] = asian;
             euro_out[(k - path_lo) * m + j] = euro;
             return j < last;
@@ -438,7 +593,7 @@ int64_t oracle_price_reference_partition(const double *params7, double S0, uint3
         OracleRNG rng(buf_words, 1u << t);                              // tpp:28
         std::vector<double> &pr_t = local[t];
         for (uint32_t i = 0; i < local_sims; ++i)
-            run_path(pr, rng, true, [&](size_t j, double asian, double euro) {
+            run_path(pr, rng, true, [&](size_t j, double asian, double euro, double) {
                 for (uint32_t o : pr.opts[j]) pr_t[o] += payoff_of(pr, o, asian, euro) / n_sims;  // tpp:40
                 return true;
             });
@@ -449,6 +604,118 @@ int64_t oracle_price_reference_partition(const double *params7, double S0, uint3
         prices[o] = s;
     }
     return (int64_t)local_sims * nt;
+}
+
+
+/*
+ * E[(G - K)^+] of the control variate for every Asian option (kind 0), the
+ * other options 0; undiscounted.  The same step modes as oracle_price_paths.
+ */
+int oracle_geo_calls(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
+                     const uint8_t *kind, uint32_t step_mode, uint32_t steps, double steps_per_year, double *out) {
+    Problem pr;
+    std::vector<uint64_t> np(n_opts, 1);
+    int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, np.data(), step_mode, steps, steps_per_year);
+    if (rc) return rc;
+    std::vector<double> dts, c;
+    for (size_t j = 0; j < pr.T.size(); ++j) {
+        std::vector<double> K;
+        for (uint32_t o : pr.opts[j]) K.push_back(strike[o]);
+        std::vector<double> res(K.size());
+        cv_schedule(pr, j, dts, c);
+        cv_geo_calls(pr.p, S0, dts, c, K.data(), K.size(), res.data(), nullptr);
+        for (size_t i = 0; i < K.size(); ++i) out[pr.opts[j][i]] = kind[pr.opts[j][i]] == 0 ? res[i] : 0.;
+    }
+    return 0;
+}
+
+/*
+ * oracle_price_paths with the geometric control variate on the Asian
+ * options.  Per Asian option the paths give the sums of a = (A - K)^+,
+ * g = (G - K)^+ and d = a - g; Cov(a, g) = (Var a + Var g - Var d) / 2,
+ * beta = Cov / Var g, and the price is exp(-r T) (mean a - beta (mean g -
+ * E[g])) with the standard error of a - beta g.  Europeans as before.
+ */
+int oracle_price_paths_cv(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
+                          const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
+                          double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                          uint64_t path_hi, int n_threads, double *price, double *stderr_out) {
+    Problem pr;
+    int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
+    if (rc) return rc;
+    if (block_words == 0 || (block_words * 8) % 128 != 0) return 4;
+    std::vector<double> eg(n_opts, 0.);
+    rc = oracle_geo_calls(params7, S0, n_opts, strike, T, kind, step_mode, steps, steps_per_year, eg.data());
+    if (rc) return rc;
+    std::vector<uint64_t> mat_paths(pr.T.size(), 0);
+    for (size_t j = 0; j < pr.T.size(); ++j)
+        for (uint32_t o : pr.opts[j]) mat_paths[j] = std::max(mat_paths[j], n_paths[o]);
+    const uint64_t n_max = *std::max_element(mat_paths.begin(), mat_paths.end());
+    path_hi = std::min(path_hi, n_max);
+    const int nt = n_threads > 0 ? n_threads : 1;
+    // per thread: a sums (ExactSums [o]), g sums (ExactSums [o]), d sums (SignedSums [o])
+    std::vector<ExactSums> pa(nt, ExactSums(n_opts)), pg(nt, ExactSums(n_opts));
+    std::vector<SignedSums> pd(nt, SignedSums(n_opts));
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+    for (int64_t k = (int64_t)path_lo; k < (int64_t)path_hi; ++k) {
+#ifdef _OPENMP
+        const int tn = omp_get_thread_num();
+#else
+        const int tn = 0;
+#endif
+        size_t last = 0;
+        for (size_t j = 0; j < pr.T.size(); ++j)
+            if (mat_paths[j] > (uint64_t)k) last = j;
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        run_path(pr, rng, false, [&](size_t j, double asian, double euro, double geo) {
+            for (uint32_t o : pr.opts[j]) {
+                if ((uint64_t)k >= n_paths[o]) continue;
+                const double a = payoff_of(pr, o, asian, euro);
+                pa[tn].add(o, a);
+                if (pr.kind[o] == 0) {
+                    const double g = std::max(0., geo - pr.strike[o]);
+                    pg[tn].add(o, g);
+                    pd[tn].add(o, a - g);
+                }
+            }
+            return j < last;
+        });
+    }
+    for (int t = 1; t < nt; ++t) {
+        pa[0].merge(pa[t]);
+        pg[0].merge(pg[t]);
+        for (size_t i = 0; i < pd[0].l.size(); ++i) pd[0].l[i] += pd[t].l[i];
+    }
+    for (uint32_t o = 0; o < n_opts; ++o) {
+        const uint64_t hi = std::min<uint64_t>(n_paths[o], path_hi);
+        const uint64_t cnt = hi > path_lo ? hi - path_lo : 0;
+        const long double n = (long double)cnt;
+        const double disc = std::exp(-pr.p.r * T[o]);
+        auto moments = [&](const uint64_t *d, bool biased, long double &mean, long double &var) {
+            __int128 s1 = (__int128)ExactSums::value(d);
+            if (biased) s1 -= (__int128)cnt << 63;
+            mean = cnt ? ((long double)s1 / 0x1p40L) / n : 0.L;
+            const long double m2 = cnt ? ((long double)ExactSums::value(d + 3) / 0x1p24L) / n : 0.L;
+            var = cnt > 1 ? (m2 - mean * mean) * n / (n - 1) : 0.L;
+            if (var < 0) var = 0;
+        };
+        long double ma, va;
+        moments(&pa[0].l[6 * (size_t)o], false, ma, va);
+        long double mean = ma, var = va;
+        if (pr.kind[o] == 0) {
+            long double mg, vg, md, vd;
+            moments(&pg[0].l[6 * (size_t)o], false, mg, vg);
+            moments(&pd[0].l[6 * (size_t)o], true, md, vd);
+            const long double cov = (va + vg - vd) / 2;
+            const long double beta = vg > 0 ? cov / vg : 0.L;
+            mean = ma - beta * (mg - (long double)eg[o]);
+            var = vg > 0 ? va - cov * cov / vg : va;
+            if (var < 0) var = 0;
+        }
+        price[o] = disc * (double)mean;
+        if (stderr_out) stderr_out[o] = cnt ? disc * std::sqrt((double)(var / n)) : 0.0;
+    }
+    return 0;
 }
 
 } // extern "C"

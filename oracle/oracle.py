@@ -143,6 +143,37 @@ def branch_counts(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536
     return int(counts[0]), int(counts[1])
 
 
+def geo_calls(params7, S0, strike, T, kind, *, step_mode=0, steps=252, steps_per_year=252.0):
+    """E[(G - K)^+] of the geometric control variate per Asian option (0 for the others), undiscounted."""
+    strike, T, kind, _ = _opts(strike, T, kind, None, 1)
+    p = np.ascontiguousarray(params7, dtype=np.float64)
+    out = np.zeros(len(strike))
+    rc = lib().oracle_geo_calls(_p(p), C.c_double(S0), C.c_uint32(len(strike)), _p(strike), _p(T), _p(kind),
+                                C.c_uint32(step_mode), C.c_uint32(steps), C.c_double(steps_per_year), _p(out))
+    if rc != 0:
+        raise ValueError(f"oracle_geo_calls failed: {rc}")
+    return out
+
+
+def price_paths_cv(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
+                   steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=None, threads=None):
+    """price_paths with the geometric control variate on the Asian options: (price, stderr)."""
+    strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
+    p = np.ascontiguousarray(params7, dtype=np.float64)
+    n = len(strike)
+    price, se = np.zeros(n), np.zeros(n)
+    hi = int(n_paths.max()) if path_hi is None else int(path_hi)
+    th = threads or os.cpu_count() or 1
+    rc = lib().oracle_price_paths_cv(_p(p), C.c_double(S0), C.c_uint32(n), _p(strike), _p(T), _p(kind),
+                                     _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps),
+                                     C.c_double(steps_per_year), C.c_uint32(seed & 0xFFFFFFFF),
+                                     C.c_uint32(block_words), C.c_uint64(path_lo), C.c_uint64(hi), C.c_int(th),
+                                     _p(price), _p(se))
+    if rc != 0:
+        raise ValueError(f"oracle_price_paths_cv failed: {rc}")
+    return price, se
+
+
 def path_finals(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
                 steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=64):
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)

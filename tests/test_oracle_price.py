@@ -105,3 +105,26 @@ def test_branch_counts_walk_the_reference_step_count(oracle):
     q1, n1 = oracle.branch_counts(base, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42, path_hi=200)
     q2, n2 = oracle.branch_counts(base, 100.0, [100.0], [1.0], [0], n_default=512, steps=252, seed=42, path_lo=200)
     assert (q1 + q2, n1 + n2) == (q, n)
+
+
+def test_geometric_control_variate_agrees_with_plain_estimator(oracle):
+    # the control variate's estimate is the plain one plus a zero-mean
+    # correction: within a few plain standard errors, with a much smaller
+    # standard error on the Asian options; Europeans untouched
+    from hestonexotics_gb300 import workloads as W
+    rq, cfg = W.single_chain(n_paths=1 << 14)
+    o = rq.options
+    args = (rq.params.as_array(), rq.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths)
+    kw = dict(n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps, steps_per_year=cfg.steps_per_year,
+              seed=rq.seed)
+    p, se, _ = oracle.price_paths(*args, **kw)
+    pc, sec = oracle.price_paths_cv(*args, **kw)
+    asian = o.payoff == 0
+    np.testing.assert_array_equal(pc[~asian], p[~asian])
+    np.testing.assert_array_equal(sec[~asian], se[~asian])
+    liquid = asian & (p > 0.05)          # enough paths in the money for the regression
+    z = np.abs(pc - p)[liquid] / se[liquid]
+    assert z.max() < 4.0, z.max()
+    assert np.median(se[liquid] / sec[liquid]) > 5.0
+    eg = oracle.geo_calls(*args[:5], step_mode=cfg.step_mode, steps=cfg.steps, steps_per_year=cfg.steps_per_year)
+    assert np.all(eg[~asian] == 0.0) and np.all(eg[asian] >= -1e-9) and np.all(eg[asian] < rq.S0)
