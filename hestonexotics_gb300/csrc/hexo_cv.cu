@@ -49,9 +49,9 @@ __device__ __forceinline__ cd cadd(cd a, cd b) { return {a.x + b.x, a.y + b.y}; 
 __device__ __forceinline__ cd csub(cd a, cd b) { return {a.x - b.x, a.y - b.y}; }
 __device__ __forceinline__ cd cmul(cd a, cd b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 __device__ __forceinline__ cd cscale(cd a, double s) { return {a.x * s, a.y * s}; }
-__device__ __forceinline__ cd cdiv(cd a, cd b) {
-    const double d = b.x * b.x + b.y * b.y;
-    return {(a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d};
+__device__ __forceinline__ cd cdiv(cd a, cd b) {   // one FP64 division (slow on this GPU) per quotient
+    const double d = 1.0 / (b.x * b.x + b.y * b.y);
+    return {(a.x * b.x + a.y * b.y) * d, (a.y * b.x - a.x * b.y) * d};
 }
 __device__ __forceinline__ cd cexp(cd a) {
     double s, c;
@@ -261,8 +261,10 @@ cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32
         if (e == cudaSuccess) e = upload(nodes, d_nodes, st);
         if (e == cudaSuccess) e = cudaMalloc(&d_phi, mats.size() * (kCvNodes + 1) * sizeof(double2));
         if (e == cudaSuccess) {
+            // one warp per block: a single request's few hundred threads spread over as many SMs
+            // as possible (the recursion is bound by each SM's FP64 pipe)
             const uint32_t n_thr = (uint32_t)mats.size() * (kCvNodes + 1);
-            cv_cf_kernel<<<(n_thr + 127) / 128, 128, 0, st>>>(d_mats, (uint32_t)mats.size(), d_steps, d_nodes, d_phi);
+            cv_cf_kernel<<<(n_thr + 31) / 32, 32, 0, st>>>(d_mats, (uint32_t)mats.size(), d_steps, d_nodes, d_phi);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
