@@ -418,7 +418,7 @@ hexo_status hexo_batch_info_get(hexo_batch *b, hexo_batch_info *info) {
     info->n_paths = bp.n_paths;
     info->n_tiles = (uint32_t)bp.tiles.size();
     info->n_sets = (uint32_t)bp.sets.size();
-    info->n_options = bp.n_out;
+    info->n_options = bp.n_out - 2u * (uint32_t)bp.cv.size();   // without the control variate's internal slots
     info->block = bp.shape.block;
     info->paths_per_thread = bp.shape.ppt;
     info->unroll = bp.shape.unroll;
@@ -512,7 +512,7 @@ hexo_status hexo_plan_stats_get(const hexo_request *reqs, uint32_t n_reqs, const
     out->n_maturities = n_mats;
     out->n_segments = n_segs;
     out->n_tiles = (uint32_t)bp.tiles.size();
-    out->n_options = bp.n_out;
+    out->n_options = base;   // the requests' options (not the control variate's internal slots)
     return HEXO_OK;
 }
 

@@ -81,3 +81,14 @@ def test_control_variate_unsupported_paths(engine):
     cfg.control_variate = 2
     with pytest.raises(HexoError):
         engine.price(req.params, req.S0, req.options, cfg)
+
+
+def test_control_variate_through_the_server(engine):
+    reqs, cfg = W.uneven_batch(n_sets=6, seed=11, path_scale=1 / 256, precision=E.FP32)
+    cfg.control_variate = 1
+    alone = [engine.price_batch([rq], cfg)[0] for rq in reqs]
+    with engine.server(cfg, max_batch_requests=3, max_inflight=2) as srv:
+        mixed = [srv.wait(t) for t in [srv.submit(rq) for rq in reqs]]
+    for (pa, sa), (pm, sm) in zip(alone, mixed):
+        np.testing.assert_array_equal(pa, pm)
+        np.testing.assert_array_equal(sa, sm)
