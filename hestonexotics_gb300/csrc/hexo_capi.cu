@@ -105,7 +105,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_acc_sum = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_price = take(n_out * sizeof(double));
     const size_t o_se = take(n_out * sizeof(double));
-    const size_t o_ctl = take(kCtlBytes);   // queue head, error flags, quadratic-branch steps
+    const size_t o_ctl = take(kCtlBytes);   // queue head, error flags, exponential-branch steps
     db.bytes = off;
     cudaError_t e = cudaSuccess;
     if (db.dmem == nullptr || db.dcap < db.bytes) {
@@ -149,7 +149,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     db.d_acc_sum = reinterpret_cast<unsigned long long *>(d + o_acc_sum);
     a.queue = reinterpret_cast<unsigned int *>(d + o_ctl);
     a.error = reinterpret_cast<int *>(d + o_ctl + sizeof(uint32_t));
-    a.quad_steps = reinterpret_cast<unsigned long long *>(d + o_ctl + 2 * sizeof(uint32_t));
+    a.exp_steps = reinterpret_cast<unsigned long long *>(d + o_ctl + 2 * sizeof(uint32_t));
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
     db.d_disc = reinterpret_cast<double *>(d + o_disc);
     db.d_price = reinterpret_cast<double *>(d + o_price);
@@ -428,7 +428,9 @@ hexo_status hexo_batch_info_get(hexo_batch *b, hexo_batch_info *info) {
     info->d2h_bytes = (uint64_t)bp.n_out * 2 * sizeof(double) + kCtlBytes;
     float ms = 0.0f;
     info->last_kernel_ms = cudaEventElapsedTime(&ms, b->db.ev_k0, b->db.ev_k1) == cudaSuccess ? (double)ms : -1.0;
-    std::memcpy(&info->quad_steps, b->db.h_ctl + 2, sizeof(uint64_t));
+    uint64_t exp_steps = 0;   // counted by the kernels; every other executed step took the quadratic branch
+    std::memcpy(&exp_steps, b->db.h_ctl + 2, sizeof(uint64_t));
+    info->quad_steps = bp.executed_path_steps - std::min(exp_steps, bp.executed_path_steps);
     return HEXO_OK;
 }
 

@@ -295,7 +295,6 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         const double theta = S.theta;
         const float S0f = S.f_S0, rf = S.f_r;
         uint32_t win_base = 0;   // first set option of the staging window
-        uint32_t n_quad = 0;     // this thread's quadratic-branch steps of active paths in the tile
 
         dev::Shishua g[PPT];
         dev::RngLane c[PPT];
@@ -329,10 +328,8 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
                     dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
-                    bool quad;
-                    if constexpr (kF32) quad = qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
-                    else quad = qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
-                    n_quad += (active[p] && quad) ? 1u : 0u;
+                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
+                    else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
                     if constexpr (kCV) {
                         yp[p] = yc[p];   // FP32: the exponent of X / S0 that qe_step used
                         if constexpr (kF32) yc[p] = __fmaf_rn(rf, pv[p].v, pv[p].lx);
@@ -394,9 +391,13 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             }
         }
         flush(S, win_base);
-        if (a.quad_steps != nullptr) {   // branch mix of the launch, one atomic per warp and tile
-            const uint32_t wq = __reduce_add_sync(0xffffffffu, n_quad);
-            if (lane == 0u && wq != 0u) atomicAdd(a.quad_steps, (unsigned long long)wq);
+        if (a.exp_steps != nullptr) {   // branch mix: each exponential-branch step drew one uniform
+            uint32_t n_exp = 0;
+#pragma unroll
+            for (int p = 0; p < PPT; ++p)
+                if (active[p]) n_exp += c[p].u_blocks * (uint32_t)kRngWords + c[p].ucur;
+            const uint32_t we = __reduce_add_sync(0xffffffffu, n_exp);
+            if (lane == 0u && we != 0u) atomicAdd(a.exp_steps, (unsigned long long)we);
         }
     }
 }

@@ -20,7 +20,7 @@ constexpr uint32_t kLimbMask = (1u << kLimbBits) - 1u;
 constexpr int kRngWords = 16;        // words per RNG buffer (one SHISHUA block)
 constexpr uint32_t kConvQueue = 96;                    // per warp: queued conversion items
 constexpr uint32_t kWarpScratchBytes = kConvQueue * 2; // per warp: the queue
-// per launch control block: tile queue head (u32), error flags (u32), quadratic-branch steps (u64)
+// per launch control block: tile queue head (u32), error flags (u32), exponential-branch steps (u64)
 constexpr size_t kCtlBytes = 16;
 constexpr int kRingSlots = 3;        // per path: normal buffer, uniform buffer, one look-ahead block
 
@@ -101,7 +101,7 @@ struct KernelArgs {
     uint64_t acc_slot_stride;
     unsigned int *queue;     // [0] tile queue head
     int *error;              // [0] error flags (bit 0: non-finite payoff, bit 1: fixed-point range)
-    unsigned long long *quad_steps; // [0] QE steps of active paths on the quadratic branch, or null
+    unsigned long long *exp_steps;  // [0] QE steps of active paths on the exponential branch, or null
     double *dbg_asian;       // optional per-path final values (debug): [(k - dbg_lo) * dbg_mats + j]
     double *dbg_euro;
     uint64_t dbg_lo;
