@@ -1,6 +1,6 @@
 """The QE branch mix the kernels report, against the oracle's walk.
 
-Each launch counts the QE steps of its active paths that took the quadratic
+Each launch reports the QE steps of its active paths that took the quadratic
 branch (HSimulation.tpp:63-68; the rest took the exponential one,
 tpp:70-73).  With every option of a request on the same path count, each
 path is walked to the same last maturity by the kernel and by the oracle,
