@@ -74,11 +74,11 @@ def alg_ops_per_path_step(p: float) -> dict:
             "int32_alu": 2.0 * SHISHUA_ALU_PER_WORD}
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
-# Nsight Compute capture of this workload at 1/16 of its paths (129.4 MB +
-# 87.0 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
+# Nsight Compute capture of this workload at 1/16 of its paths (129.0 MB +
+# 87.3 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
 # traffic is the CTA-private sum slots a launch touches plus the descriptors;
 # it does not grow with the path count, so it is reported unscaled.
-PATHS_KERNEL_DRAM_BYTES = 129.4e6 + 87.0e6
+PATHS_KERNEL_DRAM_BYTES = 129.0e6 + 87.3e6
 
 
 def dist_env():
