@@ -144,6 +144,20 @@ def test_uneven_batch_plans(lib):
     assert st.executed_path_steps >= st.nominal_path_steps > 0
 
 
+def test_control_variate_plans(lib):
+    # the control variate adds internal slots but neither options nor steps
+    reqs, cfg = W.uneven_batch(n_sets=4, path_scale=1 / 64)
+    rc0, st0 = _stats(lib, reqs, cfg)
+    cfg.control_variate = 1
+    rc1, st1 = _stats(lib, reqs, cfg)
+    assert rc0 == rc1 == 0
+    assert st1.n_options == st0.n_options == sum(len(r.options) for r in reqs)
+    assert (st1.nominal_path_steps, st1.executed_path_steps) == (st0.nominal_path_steps, st0.executed_path_steps)
+    cfg.control_variate = 2
+    rc2, _ = _stats(lib, reqs, cfg)
+    assert rc2 == 1  # HEXO_ERR_INVALID
+
+
 @pytest.mark.parametrize("bad", [
     dict(v0=float("nan")), dict(theta=0.0), dict(kappa=-1.0), dict(sigma=0.0), dict(rho=1.5)])
 def test_invalid_parameters_rejected(lib, bad):
