@@ -79,3 +79,20 @@ def test_normals_random_words(engine, oracle):
     want = oracle.normals(w)
     bad = np.flatnonzero(got.view(np.uint64) != want.view(np.uint64))
     assert bad.size == 0, (bad[:5], w[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def test_draw_moments_across_streams(engine):
+    # moments of the per-path streams the kernels use (RNG(16, seed + k)),
+    # 4096 streams x 2048 draws of each kind, within 5 standard errors;
+    # stream means must not drift with k
+    n_streams, m = 4096, 2048
+    kinds = np.concatenate([np.ones(m, dtype=np.uint8), np.zeros(m, dtype=np.uint8)])
+    d = engine.rng_draws(77, n_streams, kinds)
+    u, z = d[:, :m], d[:, m:]
+    n = u.size
+    assert abs(u.mean() - 0.5) < 5 * np.sqrt(1 / 12 / n)
+    assert abs(u.var() - 1 / 12) < 5 * np.sqrt(1 / 180 / n)
+    assert abs(z.mean()) < 5 / np.sqrt(n)
+    assert abs(z.var() - 1.0) < 5 * np.sqrt(2.0 / n)
+    half = n_streams // 2   # first and second half of the stream indices agree
+    assert abs(z[:half].mean() - z[half:].mean()) < 5 * np.sqrt(2.0 / (n / 2))

@@ -113,3 +113,18 @@ def test_logf_elsewhere_within_two_ulps(oracle):
     xs = np.concatenate([rng.uniform(0.075, 4, 5000), np.geomspace(1e-37, 1e30, 5000)]).astype(np.float32)
     err, _, _ = _logf_err_ulps(oracle, xs)
     assert err.max() <= 2.0
+
+
+def test_draw_moments_like_the_reference_rng_test(oracle):
+    # the reference's rng_test (UnitTest.cpp:528-564) checks the mean and
+    # variance of RNG(2^20, 1) uniforms and normals; here 2^21 of each from
+    # the same generator, within 5 standard errors of the exact moments
+    n = 1 << 21
+    kinds = np.concatenate([np.ones(n, dtype=np.uint8), np.zeros(n, dtype=np.uint8)])
+    d = oracle.rng_draws(1, 1 << 20, kinds)
+    u, z = d[:n], d[n:]
+    assert abs(u.mean() - 0.5) < 5 * np.sqrt(1 / 12 / n)
+    assert abs(u.var() - 1 / 12) < 5 * np.sqrt(1 / 180 / n)
+    assert abs(z.mean()) < 5 / np.sqrt(n)
+    assert abs(z.var() - 1.0) < 5 * np.sqrt(2.0 / n)
+    assert u.min() >= 0.0 and u.max() <= 1.0
