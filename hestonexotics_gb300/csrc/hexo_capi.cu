@@ -332,12 +332,22 @@ hexo_status hexo_price_batch(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n
     if (!ctx || !cfg) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
+    NvtxRange call("hexo_price_batch");
     BatchPlan bp;
     std::vector<SetPlan> plans;
-    hexo_status s = plan_requests(ctx, reqs, n_reqs, *cfg, 0, ~0ull, bp, plans);
+    hexo_status s;
+    {
+        NvtxRange r("plan");
+        s = plan_requests(ctx, reqs, n_reqs, *cfg, 0, ~0ull, bp, plans);
+    }
     if (s != HEXO_OK) return s;
     DeviceBatch db;
-    if ((s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, db)) != HEXO_OK) return s;
+    {
+        NvtxRange r("upload");
+        s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, db);
+    }
+    if (s != HEXO_OK) return s;
+    NvtxRange r("run");
     cudaError_t e = batch_enqueue(db, ctx->stream, false);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch launch");
     if ((s = batch_wait(db)) != HEXO_OK) return s;
@@ -396,6 +406,7 @@ hexo_status hexo_batch_launch(hexo_batch *b) {
     if (!b) return HEXO_ERR_INVALID;
     hexo_ctx *ctx = b->db.ctx;
     cudaSetDevice(ctx->device);
+    NvtxRange r("hexo_batch_launch");
     cudaError_t e = cudaGraphLaunch(b->db.graph_exec, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphLaunch");
     return HEXO_OK;
@@ -404,6 +415,7 @@ hexo_status hexo_batch_launch(hexo_batch *b) {
 hexo_status hexo_batch_collect(hexo_batch *b) {
     if (!b) return HEXO_ERR_INVALID;
     cudaSetDevice(b->db.ctx->device);
+    NvtxRange r("hexo_batch_collect");
     hexo_status s = batch_wait(b->db);
     if (s != HEXO_OK) return s;
     scatter_outputs(b->db, b->reqs.data(), (uint32_t)b->reqs.size());

@@ -7,7 +7,19 @@
 #include "hexo_mc.h"
 #include "hexo_plan.h"
 
+// NVTX ranges (header-only; a profiler that injects NVTX shows them, and
+// without one they cost a null check): planning, upload, the run and result
+// collection of each host call, the server's admission and launches.
+#include <nvtx3/nvToolsExt.h>
+
 namespace hexo {
+
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // A device allocation freed on scope exit.
 struct DevBuf {

@@ -202,6 +202,7 @@ bool launch_next(hexo_server *s, std::unique_lock<std::mutex> &lk) {
     s->stream_busy[si] = true;
 
     lk.unlock();   // planning the launch and uploading do not need the queue
+    NvtxRange nvtx("hexo_server launch");
     BatchPlan bp;
     std::vector<SetPlan> plans;
     plans.reserve(batch.size());
