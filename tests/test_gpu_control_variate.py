@@ -92,3 +92,18 @@ def test_control_variate_through_the_server(engine):
     for (pa, sa), (pm, sm) in zip(alone, mixed):
         np.testing.assert_array_equal(pa, pm)
         np.testing.assert_array_equal(sa, sm)
+
+
+def test_control_variate_launch_shapes_bit_identical(engine):
+    req, cfg = W.single_chain(n_paths=5000, precision=E.FP32)
+    cfg.control_variate = 1
+    out = []
+    for block in (128, 256, 512):
+        cfg.block = block
+        out.append(engine.price(req.params, req.S0, req.options, cfg))
+    for p, se in out[1:]:
+        np.testing.assert_array_equal(p, out[0][0])
+        np.testing.assert_array_equal(se, out[0][1])
+    cfg.block, cfg.paths_per_thread = 256, 2     # the control variate runs one path per thread
+    with pytest.raises(HexoError):
+        engine.price(req.params, req.S0, req.options, cfg)
