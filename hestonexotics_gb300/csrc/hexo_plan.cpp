@@ -184,10 +184,9 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
 }
 
 int last_maturity(const SetPlan &sp, uint64_t k) {
-    int jl = -1;
-    for (size_t j = 0; j < sp.mats.size(); ++j)
-        if (sp.thr[j] > k) jl = (int)j;
-    return jl;
+    // thr is non-increasing, so the maturities path k reaches are a prefix
+    const auto end = sp.thr.begin() + (long)sp.mats.size();
+    return (int)(std::partition_point(sp.thr.begin(), end, [k](uint64_t t) { return t > k; }) - sp.thr.begin()) - 1;
 }
 
 void plan_work(const SetPlan &sp, uint64_t &nominal, uint64_t &executed, uint32_t paths_per_tile) {
@@ -247,9 +246,12 @@ void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_b
 }
 
 void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans) {
-    struct Costed { TileDesc t; uint64_t cost; };
+    struct Costed { TileDesc t; uint64_t cost; uint64_t order; };
     std::vector<Costed> all;
     const uint32_t P = b.shape.paths_per_tile();
+    size_t n_tiles = 0;
+    for (const SetPlan &sp : plans) n_tiles += (size_t)((sp.path_hi - sp.path_lo + P - 1) / P);
+    all.reserve(n_tiles);
     b.nominal_path_steps = 0;
     b.executed_path_steps = 0;
     b.n_paths = 0;
@@ -269,10 +271,14 @@ void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans) {
             c.t.seg_count = sp.seg_of_mat[jl] + 1;
             c.cost = sp.steps_to_mat[jl] * (std::min<uint64_t>(k0 + P, sp.path_hi) - k0) +
                      (uint64_t)(sp.mats.size() + sp.opts.size());
+            c.order = all.size();
             all.push_back(c);
         }
     }
-    std::stable_sort(all.begin(), all.end(), [](const Costed &x, const Costed &y) { return x.cost > y.cost; });
+    // longest first; ties keep their planning order
+    std::sort(all.begin(), all.end(), [](const Costed &x, const Costed &y) {
+        return x.cost != y.cost ? x.cost > y.cost : x.order < y.order;
+    });
     b.tiles.clear();
     b.tiles.reserve(all.size());
     for (const Costed &c : all) b.tiles.push_back(c.t);
