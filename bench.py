@@ -289,7 +289,7 @@ def run_configs_report(eng):
     grid).  Per form: end-to-end path-steps/s of one hexo_price call (host
     buffers in and out, median of 5 after a warm-up) and the path kernel's
     own time; beside them the oracle port on all host cores with the same
-    per-path streams (median of 3), and, for the plain Asian, the port of
+    per-path streams (median of 5), and, for the plain Asian, the port of
     the reference's own thread partition (price()'s n / threads paths per
     thread from one RNG(2^20, 1 << tid) each, HSimulation.tpp:23-29)."""
     from oracle import oracle as O
@@ -340,7 +340,7 @@ def run_configs_report(eng):
         rq, cfg = make(FP64)
         row["nominal_path_steps"] = nominal
         ts = []
-        for _ in range(3):
+        for _ in range(5):
             t0 = time.perf_counter()
             _oracle_price_fast(O, rq, cfg, threads)
             ts.append(time.perf_counter() - t0)
@@ -349,7 +349,7 @@ def run_configs_report(eng):
         if name.startswith("plain_asian"):
             o = rq.options
             ts = []
-            for _ in range(3):
+            for _ in range(5):
                 t0 = time.perf_counter()
                 O.price_reference_partition(rq.params.as_array(), rq.S0, o.strike, o.T, o.payoff.astype(np.uint8),
                                             cfg.steps, cfg.n_paths, n_threads=threads, omp_threads=threads,
