@@ -2,7 +2,7 @@
  * ORACLE / TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement ("port") of the reference's Monte Carlo pricing path, used
- * as the parity checker for the GPU engine and as the timed CPU baseline.
+ * as the oracle of the GPU engine's parity tests and as the timed CPU baseline.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
  * it; the product never links or calls it.
  *
@@ -32,7 +32,7 @@
  *                    the QE steps on the quadratic branch (tpp:63-68).
  *
  * Built twice by oracle/Makefile: liboracle.so (-O2 -ffp-contract=off, the
- * parity checker) and liboracle_fast.so (the reference's release flags minus
+ * parity tests' oracle) and liboracle_fast.so (the reference's release flags minus
  * -march=native, the timed CPU baseline).  as241.c is always compiled
  * without fast-math, as the reference compiles as241.f90.
  */

@@ -3,8 +3,8 @@
 ctypes wrapper over the CPU oracle (oracle/_build/liboracle.so, the port of
 the reference's pricing path) and, where it was built, over
 oracle/_ref/libhexo_ref.so (the reference's own sources).  Imported only by
-tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the
-checker; the product never imports it.
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, to check
+results against; the product never imports it.
 """
 from __future__ import annotations
 
