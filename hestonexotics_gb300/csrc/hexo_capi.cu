@@ -314,6 +314,8 @@ hexo_status hexo_ctx_destroy(hexo_ctx *ctx) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
+    if (ctx->arena_d) cudaFree(ctx->arena_d);
+    if (ctx->arena_h) cudaFreeHost(ctx->arena_h);
     delete ctx;
     return HEXO_OK;
 }
@@ -342,6 +344,7 @@ hexo_status hexo_price_batch(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n
     }
     if (s != HEXO_OK) return s;
     DeviceBatch db;
+    ArenaLoan loan(ctx, db);
     {
         NvtxRange r("upload");
         s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, db);
@@ -475,6 +478,7 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
     hexo_status s = plan_requests(ctx, &r, 1, *cfg, path_lo, path_hi, bp, plans);
     if (s != HEXO_OK) return s;
     DeviceBatch db;
+    ArenaLoan loan(ctx, db);
     if ((s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, db)) != HEXO_OK) return s;
     cudaError_t e = batch_enqueue(db, ctx->stream, true);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "partial launch");

@@ -74,6 +74,11 @@ struct hexo_ctx {
     std::mutex run_mu;                        // one launch sequence at a time on the stream
     std::mutex err_mu;
     std::string last_error;
+    // device and pinned host memory of the last one-shot call, reused by the
+    // next (guarded by run_mu; freed by hexo_ctx_destroy): no allocation, and
+    // so no device synchronisation, per call once the largest batch was seen
+    void *arena_d = nullptr, *arena_h = nullptr;
+    size_t arena_dcap = 0, arena_hcap = 0;
 };
 
 struct hexo_batch {
@@ -82,6 +87,33 @@ struct hexo_batch {
 };
 
 namespace hexo {
+// Lends the context's arena to a one-shot batch and keeps whatever larger
+// memory the batch allocated instead (declare after the DeviceBatch).
+struct ArenaLoan {
+    hexo_ctx *ctx;
+    DeviceBatch &db;
+    ArenaLoan(hexo_ctx *c, DeviceBatch &d) : ctx(c), db(d) {
+        db.dmem = ctx->arena_d; db.dcap = ctx->arena_dcap;
+        db.hmem = ctx->arena_h; db.hcap = ctx->arena_hcap;
+        db.own_d = db.own_h = false;
+    }
+    ~ArenaLoan() {
+        if (db.own_d && db.dmem) {
+            if (ctx->arena_d) cudaFree(ctx->arena_d);
+            ctx->arena_d = db.dmem;
+            ctx->arena_dcap = db.dcap;
+        }
+        if (db.own_h && db.hmem) {
+            if (ctx->arena_h) cudaFreeHost(ctx->arena_h);
+            ctx->arena_h = db.hmem;
+            ctx->arena_hcap = db.hcap;
+        }
+        db.own_d = db.own_h = false;
+    }
+    ArenaLoan(const ArenaLoan &) = delete;
+    ArenaLoan &operator=(const ArenaLoan &) = delete;
+};
+
 hexo_status ctx_fail(hexo_ctx *ctx, hexo_status s, const std::string &msg);
 hexo_status cuda_fail(hexo_ctx *ctx, cudaError_t e, const char *what);
 LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg);
