@@ -72,6 +72,9 @@ typedef struct hexo_ctx_opts {
     uint32_t flags;             /* reserved, 0 */
 } hexo_ctx_opts;
 
+/* A context keeps the device and pinned host memory of its largest one-shot
+ * call (hexo_price, hexo_price_batch, hexo_price_partial) for the next one,
+ * so repeated calls allocate nothing; hexo_ctx_destroy frees it. */
 hexo_status hexo_ctx_create(hexo_ctx **out, const hexo_ctx_opts *opts /* NULL = defaults */);
 /* Waits for the context's work and frees it.  Batches, servers and
  * calibration handles made on the context must be destroyed first. */
