@@ -114,6 +114,21 @@ struct ArenaLoan {
     ArenaLoan &operator=(const ArenaLoan &) = delete;
 };
 
+// The context's device arena as scratch of at least `bytes` (grown when
+// smaller); valid until the next call on the context (hold run_mu).
+inline cudaError_t ctx_scratch(hexo_ctx *ctx, size_t bytes, void **p) {
+    if (ctx->arena_d == nullptr || ctx->arena_dcap < bytes) {
+        if (ctx->arena_d) cudaFree(ctx->arena_d);
+        ctx->arena_d = nullptr;
+        ctx->arena_dcap = 0;
+        const cudaError_t e = cudaMalloc(&ctx->arena_d, bytes ? bytes : 1);
+        if (e != cudaSuccess) { ctx->arena_d = nullptr; return e; }
+        ctx->arena_dcap = bytes;
+    }
+    *p = ctx->arena_d;
+    return cudaSuccess;
+}
+
 hexo_status ctx_fail(hexo_ctx *ctx, hexo_status s, const std::string &msg);
 hexo_status cuda_fail(hexo_ctx *ctx, cudaError_t e, const char *what);
 LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg);

@@ -443,10 +443,10 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
     const size_t o_tw = take(tw * sizeof(double2)), o_h = take(h * sizeof(double2));
     const size_t o_v = take(v * sizeof(double)), o_w = take(w * sizeof(double2));
     const size_t o_p = take(n_opt * sizeof(double)), o_g = take(any_grad ? n_opt * 5 * sizeof(double) : 0);
-    DevBuf buf;
-    cudaError_t err = buf.alloc(off);
+    void *dmem = nullptr;   // the context's arena: no allocation once it is large enough
+    cudaError_t err = ctx_scratch(ctx, off, &dmem);
     if (err != cudaSuccess) return cuda_fail(ctx, err, "cudaMalloc swift");
-    char *d = static_cast<char *>(buf.p);
+    char *d = static_cast<char *>(dmem);
     auto up = [&](size_t o, const void *src, size_t bytes) {
         return bytes ? cudaMemcpyAsync(d + o, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
     };
