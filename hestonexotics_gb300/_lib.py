@@ -47,7 +47,7 @@ class hexo_mc_cfg(C.Structure):
     _fields_ = [("n_paths", C.c_uint64), ("step_mode", C.c_uint32), ("steps", C.c_uint32),
                 ("steps_per_year", C.c_double), ("seed", C.c_uint32), ("rng_block_words", C.c_uint32),
                 ("precision", C.c_uint32), ("block", C.c_uint32), ("paths_per_thread", C.c_uint32),
-                ("unroll", C.c_uint32), ("control_variate", C.c_uint32), ("reserved", C.c_uint32)]
+                ("unroll", C.c_uint32), ("control_variate", C.c_uint32), ("stream", C.c_uint32)]
 
 
 class hexo_ctx_opts(C.Structure):
@@ -58,7 +58,7 @@ class hexo_ctx_opts(C.Structure):
 class hexo_request(C.Structure):
     _fields_ = [("params", hexo_params), ("S0", C.c_double), ("opts", C.POINTER(hexo_option)),
                 ("n_opts", C.c_uint32), ("seed", C.c_uint32), ("price_out", C.POINTER(C.c_double)),
-                ("stderr_out", C.POINTER(C.c_double))]
+                ("stderr_out", C.POINTER(C.c_double)), ("stream", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class hexo_batch_info(C.Structure):
@@ -155,7 +155,7 @@ PROTOTYPES = {
     "hexo_calib_destroy": (C.c_int, [_P]),
     "hexo_price_partial": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
-    "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.POINTER(hexo_option), C.c_uint32,
+    "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                       C.POINTER(hexo_mc_cfg), _U64, _D, _D]),
     "hexo_price_noalloc": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), _D, _D, _P]),
@@ -165,10 +165,11 @@ PROTOTYPES = {
                                      C.POINTER(hexo_mc_cfg), C.c_uint32, _U64, _D, _D, C.POINTER(C.c_uint32)]),
     "hexo_autotune": (C.c_int, [_P, C.POINTER(hexo_request), C.c_uint32, C.POINTER(hexo_mc_cfg),
                                 C.POINTER(hexo_tune_result), C.POINTER(hexo_tune_entry), C.c_uint32]),
-    "hexo_debug_rng_words": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _U64]),
-    "hexo_debug_rng_draws": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32, _D]),
+    "hexo_debug_rng_words": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _U64]),
+    "hexo_debug_rng_draws": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32,
+                                       _D]),
     "hexo_debug_normals": (C.c_int, [_P, _U64, C.c_uint64, _D]),
-    "hexo_debug_payoff_limbs": (C.c_int, [_P, _D, C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "hexo_debug_payoff_limbs": (C.c_int, [_P, _D, C.c_uint64, C.c_uint32, C.c_double, C.POINTER(C.c_uint32)]),
     "hexo_debug_pipe_peaks": (C.c_int, [_P, _D]),
     "hexo_debug_path_finals": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option),
                                          C.c_uint32, C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _D, _D,
@@ -178,7 +179,7 @@ PROTOTYPES = {
 _lib = None
 
 
-ABI_VERSION = 3   # HEXO_ABI_VERSION of include/hexo_mc.h these prototypes and structs follow
+ABI_VERSION = 4   # HEXO_ABI_VERSION of include/hexo_mc.h these prototypes and structs follow
 
 
 def load() -> C.CDLL:

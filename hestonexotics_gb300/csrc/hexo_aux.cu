@@ -14,10 +14,21 @@ cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t 
     return cudaLaunchKernel(fn, dim3(grid), dim3(sh.block), params, smem, st);
 }
 
+cudaError_t paths_smem_limit(const void *fn, int dev) {
+    if (fn == nullptr) return cudaErrorInvalidValue;
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, fn)) != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
+
 // Sums the CTA-private copies of the limbs (exact integer additions) and
 // finalises each option.
 __global__ void finalize_kernel(const unsigned long long *__restrict__ acc, uint32_t n_slots, uint64_t slot_stride,
-                                const uint64_t *__restrict__ n_paths, const double *__restrict__ disc, uint32_t n,
+                                const uint64_t *__restrict__ n_paths, const double *__restrict__ disc,
+                                const int32_t *__restrict__ pay_exp, uint32_t n,
                                 double *__restrict__ price, double *__restrict__ se,
                                 unsigned long long *__restrict__ acc_sum, const double *__restrict__ cv_eg,
                                 const uint32_t *__restrict__ cv_partner) {
@@ -41,31 +52,32 @@ __global__ void finalize_kernel(const unsigned long long *__restrict__ acc, uint
         uint64_t lg[kLimbs], ld[kLimbs];
         total(g, lg);
         total(g + 1u, ld);
-        finalize_cv(l, lg, ld, n_paths[i], disc[i], cv_eg[i], &p, &s);
+        finalize_cv(l, lg, ld, n_paths[i], disc[i], pay_exp[i], cv_eg[i], &p, &s);
     } else {
-        finalize_limbs6(l, n_paths[i], disc[i], &p, &s);
+        finalize_limbs6(l, n_paths[i], disc[i], pay_exp[i], &p, &s);
     }
     price[i] = p;
     se[i] = s;
 }
 
 cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
-                            const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
-                            unsigned long long *acc_sum, cudaStream_t st, const double *cv_eg,
-                            const uint32_t *cv_partner) {
+                            const uint64_t *n_paths, const double *disc, const int32_t *pay_exp, uint32_t n,
+                            double *price, double *se, unsigned long long *acc_sum, cudaStream_t st,
+                            const double *cv_eg, const uint32_t *cv_partner) {
     if (n == 0) return cudaSuccess;
-    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, n, price, se, acc_sum,
-                                                      cv_eg, cv_partner);
+    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, pay_exp, n, price, se,
+                                                      acc_sum, cv_eg, cv_partner);
     return cudaGetLastError();
 }
 
 // Raw stream words: block 0 is the state after initialisation with its
 // lanes reversed, then one block per round.
-__global__ void dbg_words_kernel(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out) {
+__global__ void dbg_words_kernel(uint32_t seed, uint32_t stream, uint32_t n_streams, uint32_t n_words,
+                                 uint64_t *out) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_streams) return;
     dev::Shishua g;
-    dev::sh_init(g, (uint64_t)(uint32_t)(seed + k));
+    dev::sh_init(g, (uint64_t)(uint32_t)(seed + k), (uint64_t)stream);
     uint64_t o[16];
 #pragma unroll
     for (int L = 0; L < 4; ++L)
@@ -80,7 +92,8 @@ __global__ void dbg_words_kernel(uint32_t seed, uint32_t n_streams, uint32_t n_w
 }
 
 // The two-buffer RNG through the same ring code as the path kernel.
-__global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out) {
+__global__ void dbg_draws_kernel(uint32_t seed, uint32_t stream, uint32_t n_streams, const uint8_t *kinds, uint32_t n,
+                                 double *out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t bd = blockDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     uint64_t *raw = reinterpret_cast<uint64_t *>(smem_raw);
@@ -91,7 +104,7 @@ __global__ void dbg_draws_kernel(uint32_t seed, uint32_t n_streams, const uint8_
     dev::WarpScratch ws{raw + tid - lane, nrm + tid - lane, tq_i + warp * kConvQueue, lane};
     dev::Shishua g;
     dev::RngLane c;
-    dev::rng_start<true>(g, c, r, ws, seed + k);
+    dev::rng_start<true>(g, c, r, ws, seed + k, stream);
     for (uint32_t i = 0; i < n; i += 2) {
         dev::rng_topup<true>(g, c, r, ws);   // same cadence as one QE step (two draws)
         if (i + 1 < n && kinds[i + 1] == 0) {
@@ -123,31 +136,33 @@ __global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *ou
     }
 }
 
-__global__ void dbg_limbs_kernel(const double *pay, uint64_t n, bool f32, uint32_t *out) {
+__global__ void dbg_limbs_kernel(const double *pay, uint64_t n, bool f32, int E, uint32_t *out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
-        const bool ok = f32 ? dev::limbs_add_f32((float)pay[i], l) : dev::limbs_add_f64(pay[i], l);
+        const bool ok = f32 ? dev::limbs_add_f32((float)pay[i], E + 103, l) : dev::limbs_add_f64(pay[i], E, l);
         for (int x = 0; x < kLimbs; ++x) out[i * kLimbs + x] = ok ? l[x] : 0xFFFFFFFFu;
     }
 }
 
-cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st) {
-    dbg_words_kernel<<<(n_streams + 127) / 128, 128, 0, st>>>(seed, n_streams, n_words, out);
+cudaError_t launch_dbg_words(uint32_t seed, uint32_t stream, uint32_t n_streams, uint32_t n_words, uint64_t *out,
+                             cudaStream_t st) {
+    dbg_words_kernel<<<(n_streams + 127) / 128, 128, 0, st>>>(seed, stream, n_streams, n_words, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
+cudaError_t launch_dbg_draws(uint32_t seed, uint32_t stream, uint32_t n_streams, const uint8_t *kinds, uint32_t n,
+                             double *out,
                              cudaStream_t st) {
     const uint32_t bd = 64;
     const size_t smem = (size_t)2 * kRngWords * bd * (sizeof(uint64_t) + sizeof(float)) + (bd / 32) * kWarpScratchBytes;
-    dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, n_streams, kinds, n, out);
+    dbg_draws_kernel<<<(n_streams + bd - 1) / bd, bd, smem, st>>>(seed, stream, n_streams, kinds, n, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, uint32_t *out, cudaStream_t st) {
+cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, int E, uint32_t *out, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    dbg_limbs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pay, n, f32, out);
+    dbg_limbs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pay, n, f32, E, out);
     return cudaGetLastError();
 }
 

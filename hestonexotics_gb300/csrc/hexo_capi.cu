@@ -51,9 +51,12 @@ hexo_status shape_check(hexo_ctx *ctx, bool f32, const LaunchShape &sh, size_t &
     if (fn == nullptr || sh.block == 0 || sh.block % 32 != 0 || sh.block > 512)
         return ctx_fail(ctx, HEXO_ERR_INVALID, "unsupported launch shape (block multiple of 32 up to 512, ppt/unroll in {1,2,4})");
     smem = paths_smem_bytes(sh.block, sh.ppt);
-    if (smem > ctx->smem_optin)
+    size_t smem_static = 0;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess) smem_static = fa.sharedSizeBytes;
+    if (smem + smem_static > ctx->smem_optin)
         return ctx_fail(ctx, HEXO_ERR_INVALID, "launch shape needs more shared memory than a CTA can have");
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = paths_smem_limit(fn, ctx->device);   // the same value for every caller
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaFuncSetAttribute");
     int nb = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, (int)sh.block, smem);
@@ -101,6 +104,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_tiles = take(std::max<size_t>(1, bp.tiles.size()) * sizeof(TileDesc));
     const size_t o_paths = take(n_out * sizeof(uint64_t));
     const size_t o_disc = take(n_out * sizeof(double));
+    const size_t o_pexp = take(n_out * sizeof(int32_t));
     const size_t o_acc = take((size_t)db.n_slots * n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_acc_sum = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_price = take(n_out * sizeof(double));
@@ -152,6 +156,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     a.exp_steps = reinterpret_cast<unsigned long long *>(d + o_ctl + 2 * sizeof(uint32_t));
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
     db.d_disc = reinterpret_cast<double *>(d + o_disc);
+    db.d_pexp = reinterpret_cast<int32_t *>(d + o_pexp);
     db.d_price = reinterpret_cast<double *>(d + o_price);
     db.d_se = reinterpret_cast<double *>(d + o_se);
 
@@ -166,13 +171,14 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
         (e = up(o_opts, bp.opts.data(), bp.opts.size() * sizeof(OptDesc))) != cudaSuccess ||
         (e = up(o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(TileDesc))) != cudaSuccess ||
         (e = up(o_paths, bp.opt_paths.data(), n_out * sizeof(uint64_t))) != cudaSuccess ||
-        (e = up(o_disc, bp.opt_disc.data(), n_out * sizeof(double))) != cudaSuccess)
+        (e = up(o_disc, bp.opt_disc.data(), n_out * sizeof(double))) != cudaSuccess ||
+        (e = up(o_pexp, bp.opt_pexp.data(), n_out * sizeof(int32_t))) != cudaSuccess)
         return cuda_fail(ctx, e, "upload batch");
     e = cudaStreamSynchronize(st);   // the host vectors are pageable: finish before they can change
     if (e != cudaSuccess) return cuda_fail(ctx, e, "upload batch");
     db.h2d_bytes = bp.sets.size() * sizeof(SetDesc) + bp.segs.size() * sizeof(SegDesc) +
                    bp.mats.size() * sizeof(MatDesc) + bp.opts.size() * sizeof(OptDesc) +
-                   bp.tiles.size() * sizeof(TileDesc) + n_out * (sizeof(uint64_t) + sizeof(double));
+                   bp.tiles.size() * sizeof(TileDesc) + n_out * (sizeof(uint64_t) + sizeof(double) + sizeof(int32_t));
     if ((e = cudaEventCreate(&db.ev_k0)) != cudaSuccess || (e = cudaEventCreate(&db.ev_k1)) != cudaSuccess)
         return cuda_fail(ctx, e, "cudaEventCreate");
     if (!bp.cv.empty() && (e = cv_prepare(bp, st, &db.d_cv_eg, &db.d_cv_partner)) != cudaSuccess)
@@ -196,8 +202,9 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     if (db.args.n_tiles > 0)
         if ((e = launch_paths(db.f32, db.plan.shape, db.grid, db.smem, st, db.args)) != cudaSuccess) return e;
     if ((e = cudaEventRecordWithFlags(db.ev_k1, st, rec_flags)) != cudaSuccess) return e;
-    if ((e = launch_finalize(db.args.acc, db.n_slots, db.args.acc_slot_stride, db.d_paths, db.d_disc, n_out,
-                             db.d_price, db.d_se, db.d_acc_sum, st, db.d_cv_eg, db.d_cv_partner)) != cudaSuccess)
+    if ((e = launch_finalize(db.args.acc, db.n_slots, db.args.acc_slot_stride, db.d_paths, db.d_disc, db.d_pexp,
+                             n_out, db.d_price, db.d_se, db.d_acc_sum, st, db.d_cv_eg, db.d_cv_partner)) !=
+        cudaSuccess)
         return e;
     if ((e = cudaMemcpyAsync(db.h_price, db.d_price, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_se, db.d_se, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
@@ -211,7 +218,8 @@ hexo_status batch_wait(DeviceBatch &db) {
     cudaError_t e = cudaStreamSynchronize(db.stream);
     if (e != cudaSuccess) return cuda_fail(db.ctx, e, "batch run");
     if (db.h_ctl[1] != 0u)
-        return ctx_fail(db.ctx, HEXO_ERR_NUMERIC, "a payoff was not finite or outside the fixed-point range [0, 2^23)");
+        return ctx_fail(db.ctx, HEXO_ERR_NUMERIC,
+                        "a payoff was not finite or outside the fixed-point range [0, 2^16 * 2^E), 2^(E-1) <= S0 < 2^E");
     return HEXO_OK;
 }
 
@@ -223,8 +231,8 @@ hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_re
     for (uint32_t r = 0; r < n_reqs; ++r) cv_base += reqs[r].n_opts;   // internal slots after all outputs
     for (uint32_t r = 0; r < n_reqs; ++r) {
         std::string err;
-        hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, cfg, reqs[r].seed, path_lo,
-                                 path_hi, plans[r], err);
+        hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, cfg, reqs[r].seed,
+                                 reqs[r].stream, path_lo, path_hi, plans[r], err);
         if (s != HEXO_OK) return ctx_fail(ctx, s, "request " + std::to_string(r) + ": " + err);
         batch_add(bp, plans[r], out_base, cv_base);
         out_base += reqs[r].n_opts;
@@ -367,6 +375,8 @@ hexo_status hexo_price(hexo_ctx *ctx, const hexo_params *p, double S0, const hex
     r.opts = opts;
     r.n_opts = n_opts;
     r.seed = cfg->seed;
+    r.stream = cfg->stream;
+    r.reserved = 0;
     r.price_out = price_out;
     r.stderr_out = stderr_out;
     return hexo_price_batch(ctx, &r, 1, cfg);
@@ -473,6 +483,7 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
     r.opts = opts;
     r.n_opts = n_opts;
     r.seed = cfg->seed;
+    r.stream = cfg->stream;
     BatchPlan bp;
     std::vector<SetPlan> plans;
     hexo_status s = plan_requests(ctx, &r, 1, *cfg, path_lo, path_hi, bp, plans);
@@ -487,14 +498,16 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
     return HEXO_OK;
 }
 
-hexo_status hexo_finalize_limbs(const hexo_params *p, const hexo_option *opts, uint32_t n_opts, const hexo_mc_cfg *cfg,
-                                const uint64_t *limbs, double *price_out, double *stderr_out) {
+hexo_status hexo_finalize_limbs(const hexo_params *p, double S0, const hexo_option *opts, uint32_t n_opts,
+                                const hexo_mc_cfg *cfg, const uint64_t *limbs, double *price_out, double *stderr_out) {
     if (!p || !opts || !cfg || !limbs || !price_out) return HEXO_ERR_INVALID;
+    if (!std::isfinite(S0) || !(S0 >= 0x1p-60) || !(S0 < 0x1p60)) return HEXO_ERR_INVALID;
+    const int E = pay_exponent(S0);
     for (uint32_t i = 0; i < n_opts; ++i) {
         const uint64_t n = opts[i].n_paths ? opts[i].n_paths : cfg->n_paths;
         if (n == 0) return HEXO_ERR_INVALID;
         double pr, se;
-        finalize_one(limbs + (size_t)i * kLimbs, n, std::exp(-p->r * opts[i].T), &pr, &se);
+        finalize_one(limbs + (size_t)i * kLimbs, n, std::exp(-p->r * opts[i].T), E, &pr, &se);
         price_out[i] = pr;
         if (stderr_out) stderr_out[i] = se;
     }
@@ -512,8 +525,8 @@ hexo_status hexo_plan_stats_get(const hexo_request *reqs, uint32_t n_reqs, const
     for (uint32_t r = 0; r < n_reqs; ++r) cv_base += reqs[r].n_opts;
     for (uint32_t r = 0; r < n_reqs; ++r) {
         std::string err;
-        hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, *cfg, reqs[r].seed, 0,
-                                 ~0ull, plans[r], err);
+        hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, *cfg, reqs[r].seed,
+                                 reqs[r].stream, 0, ~0ull, plans[r], err);
         if (s != HEXO_OK) return s;
         batch_add(bp, plans[r], base, cv_base);
         base += reqs[r].n_opts;
@@ -540,7 +553,7 @@ hexo_status hexo_plan_schedule(const hexo_params *p, double S0, const hexo_optio
     if (!p || !cfg || !n_mats) return HEXO_ERR_INVALID;
     SetPlan sp;
     std::string err;
-    hexo_status s = plan_set(*p, S0, opts, n_opts, *cfg, cfg->seed, 0, ~0ull, sp, err);
+    hexo_status s = plan_set(*p, S0, opts, n_opts, *cfg, cfg->seed, cfg->stream, 0, ~0ull, sp, err);
     if (s != HEXO_OK) return s;
     *n_mats = (uint32_t)sp.mats.size();
     for (uint32_t j = 0; j < *n_mats && j < cap; ++j) {
@@ -553,21 +566,22 @@ hexo_status hexo_plan_schedule(const hexo_params *p, double S0, const hexo_optio
 
 // ----------------------------------------------------------------- debug
 
-hexo_status hexo_debug_rng_words(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out) {
+hexo_status hexo_debug_rng_words(hexo_ctx *ctx, uint32_t seed, uint32_t stream, uint32_t n_streams, uint32_t n_words,
+                                 uint64_t *out) {
     if (!ctx || !out || n_streams == 0 || n_words == 0) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     DevBuf d;
     const size_t bytes = (size_t)n_streams * n_words * sizeof(uint64_t);
     cudaError_t e = d.alloc(bytes);
-    if (e == cudaSuccess) e = launch_dbg_words(seed, n_streams, n_words, (uint64_t *)d.p, ctx->stream);
+    if (e == cudaSuccess) e = launch_dbg_words(seed, stream, n_streams, n_words, (uint64_t *)d.p, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d.p, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug rng words");
 }
 
-hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n,
-                                 double *out) {
+hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t stream, uint32_t n_streams,
+                                 const uint8_t *kinds, uint32_t n, double *out) {
     if (!ctx || !out || !kinds || n_streams == 0 || n == 0) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
@@ -576,7 +590,8 @@ hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t n_stream
     cudaError_t e = dk.alloc(n);
     if (e == cudaSuccess) e = dout.alloc(bytes);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dk.p, kinds, n, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = launch_dbg_draws(seed, n_streams, (const uint8_t *)dk.p, n, (double *)dout.p, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_dbg_draws(seed, stream, n_streams, (const uint8_t *)dk.p, n, (double *)dout.p, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout.p, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug rng draws");
@@ -596,10 +611,12 @@ hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n,
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug normals");
 }
 
-hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision,
+hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision, double S0,
                                     uint32_t *out) {
     if (!ctx || !pay || !out || n == 0) return HEXO_ERR_INVALID;
     if (precision != HEXO_FP64 && precision != HEXO_FP32) return ctx_fail(ctx, HEXO_ERR_INVALID, "unknown precision");
+    if (!std::isfinite(S0) || !(S0 >= 0x1p-60) || !(S0 < 0x1p60))
+        return ctx_fail(ctx, HEXO_ERR_INVALID, "S0 must be in [2^-60, 2^60)");
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     DevBuf dp, dout;
@@ -607,7 +624,8 @@ hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n
     if (e == cudaSuccess) e = dout.alloc(n * kLimbs * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemcpyAsync(dp.p, pay, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
-        e = launch_dbg_limbs((const double *)dp.p, n, precision == HEXO_FP32, (uint32_t *)dout.p, ctx->stream);
+        e = launch_dbg_limbs((const double *)dp.p, n, precision == HEXO_FP32, pay_exponent(S0), (uint32_t *)dout.p,
+                             ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(out, dout.p, n * kLimbs * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -636,6 +654,7 @@ hexo_status hexo_debug_path_finals(hexo_ctx *ctx, const hexo_params *p, double S
     r.opts = opts;
     r.n_opts = n_opts;
     r.seed = cfg->seed;
+    r.stream = cfg->stream;
     BatchPlan bp;
     std::vector<SetPlan> plans;
     hexo_status s = plan_requests(ctx, &r, 1, *cfg, path_lo, path_hi, bp, plans);

@@ -26,24 +26,30 @@ inline const void *paths_kernel_ptr(bool f32, uint32_t ppt, uint32_t unroll, boo
 }
 cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t smem, cudaStream_t st,
                          const KernelArgs &a);
+// Sets the path kernel fn's dynamic shared-memory limit to the most it can
+// have on device dev (the opt-in maximum less its static shared memory).
+// Every entry point sets this same value before it launches fn, so one
+// caller's launch shape never lowers the limit under another's launch.
+cudaError_t paths_smem_limit(const void *fn, int dev);
 
 // Finaliser: sums the n_slots private copies of the limbs (acc_sum, when not
 // null, receives the totals) and writes price and standard error per slot.
 cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
-                            const uint64_t *n_paths, const double *disc, uint32_t n, double *price, double *se,
-                            unsigned long long *acc_sum, cudaStream_t st, const double *cv_eg = nullptr,
-                            const uint32_t *cv_partner = nullptr);
+                            const uint64_t *n_paths, const double *disc, const int32_t *pay_exp, uint32_t n,
+                            double *price, double *se, unsigned long long *acc_sum, cudaStream_t st,
+                            const double *cv_eg = nullptr, const uint32_t *cv_partner = nullptr);
 // The geometric control variate's analytic part for a planned batch:
 // E[(G - K)^+] per control-variate option into *eg and its geometric-sum slot
 // into *partner (device arrays of n_out entries, allocated here).
 cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32_t **partner);
 
 // Debug kernels.
-cudaError_t launch_dbg_words(uint32_t seed, uint32_t n_streams, uint32_t n_words, uint64_t *out, cudaStream_t st);
-cudaError_t launch_dbg_draws(uint32_t seed, uint32_t n_streams, const uint8_t *kinds, uint32_t n, double *out,
+cudaError_t launch_dbg_words(uint32_t seed, uint32_t stream, uint32_t n_streams, uint32_t n_words, uint64_t *out,
                              cudaStream_t st);
+cudaError_t launch_dbg_draws(uint32_t seed, uint32_t stream, uint32_t n_streams, const uint8_t *kinds, uint32_t n,
+                             double *out, cudaStream_t st);
 cudaError_t launch_dbg_normals(const uint64_t *words, uint64_t n, double *out, cudaStream_t st);
-cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, uint32_t *out, cudaStream_t st);
+cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, int E, uint32_t *out, cudaStream_t st);
 cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out5);
 
 } // namespace hexo

@@ -18,9 +18,17 @@
 // cudaGetSymbolAddress (the array's name on the host is a stand-in, not a
 // device address); that lookup happens on the first call on each device,
 // with the device current, so the first call on a device should come before
-// any stream capture.  Every call shares the array and the call clears what
-// must start at zero; calls whose work overlaps on the GPU (from several
+// any stream capture.  A call blocks until its results are on the host, so
+// it refuses a stream that is being captured (HEXO_ERR_UNSUPPORTED) before
+// it enqueues anything.  Every call shares the array and the call clears
+// what must start at zero; calls whose work overlaps on the GPU (from several
 // threads or streams) race on it and must be serialised by the caller.
+//
+// The path kernels' dynamic shared-memory limit is a per-kernel attribute
+// that every entry point of the library sets; all of them set it to the
+// same value, the device's opt-in maximum less the kernel's static shared
+// memory (paths_smem_limit), so no caller can lower it under another's
+// launch.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -50,7 +58,8 @@ constexpr size_t kOffOpts = kOffMats + na_align(kNaMaxOptions * sizeof(MatDesc))
 constexpr size_t kOffTiles = kOffOpts + na_align(kNaMaxOptions * sizeof(OptDesc));
 constexpr size_t kOffPaths = kOffTiles + na_align(kNaMaxTiles * sizeof(TileDesc));
 constexpr size_t kOffDisc = kOffPaths + na_align(kNaMaxOptions * sizeof(uint64_t));
-constexpr size_t kOffAcc = kOffDisc + na_align(kNaMaxOptions * sizeof(double));
+constexpr size_t kOffPexp = kOffDisc + na_align(kNaMaxOptions * sizeof(double));
+constexpr size_t kOffAcc = kOffPexp + na_align(kNaMaxOptions * sizeof(int32_t));
 constexpr size_t kOffPrice = kOffAcc + na_align(kNaMaxOptions * kLimbs * sizeof(unsigned long long));
 constexpr size_t kOffSe = kOffPrice + na_align(kNaMaxOptions * sizeof(double));
 constexpr size_t kOffCtl = kOffSe + na_align(kNaMaxOptions * sizeof(double));
@@ -87,7 +96,7 @@ hexo_status na_setup(int dev, bool f32, unsigned char **scratch, uint32_t *grid_
         for (int k = 0; k < 2; ++k) {
             const void *fn = paths_kernel_ptr(k == 1, 1, 1);
             int nb = 0;
-            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            if (paths_smem_limit(fn, dev) != cudaSuccess ||
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, (int)kNaBlock, smem) != cudaSuccess || nb <= 0)
                 return HEXO_ERR_CUDA;
             g_na_ctas[k][dev] = (uint32_t)nb;
@@ -143,7 +152,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
         if (!std::isfinite(x)) return HEXO_ERR_INVALID;
     if (!(p.v0 >= 0.0) || !(p.theta > 0.0) || !(p.kappa > 0.0) || !(p.sigma > 0.0) || !(std::fabs(p.rho) <= 1.0))
         return HEXO_ERR_INVALID;
-    if (!std::isfinite(S0) || !(S0 > 0.0)) return HEXO_ERR_INVALID;
+    if (!std::isfinite(S0) || !(S0 >= 0x1p-60) || !(S0 < 0x1p60)) return HEXO_ERR_INVALID;
     if ((cfg->rng_block_words ? cfg->rng_block_words : 16u) != 16u) return HEXO_ERR_UNSUPPORTED;
     if (cfg->step_mode > 1u || cfg->precision > 1u) return HEXO_ERR_INVALID;
     if (cfg->step_mode == HEXO_STEP_REFERENCE && cfg->steps == 0) return HEXO_ERR_INVALID;
@@ -168,6 +177,8 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     OptDesc od[kNaMaxOptions];
     uint64_t opt_paths[kNaMaxOptions];
     double opt_disc[kNaMaxOptions];
+    int32_t opt_pexp[kNaMaxOptions];
+    const int32_t E = pay_exponent(S0);
     uint32_t mat_steps[kNaMaxOptions];
     uint64_t mat_paths[kNaMaxOptions];
     uint32_t seg_of_mat[kNaMaxOptions];
@@ -197,6 +208,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
         od[r].out_index = i;
         opt_paths[i] = od[r].n_paths;
         opt_disc[i] = std::exp(-p.r * opts[i].T);
+        opt_pexp[i] = E;
         mats[m - 1].opt_end = r + 1;
         mat_paths[m - 1] = std::max(mat_paths[m - 1], od[r].n_paths);
     }
@@ -248,6 +260,8 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     sd.f_r = (float)(p.rho / p.sigma);
     ds_split(p.v0, sd.ds_v0);
     sd.seed = cfg->seed;
+    sd.stream = cfg->stream;
+    sd.pay_exp = E;
     sd.seg_count = n_segs;
     sd.mat_count = m;
     sd.opt_count = n_opts;
@@ -257,11 +271,14 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     // ---- device side: everything lives in the static scratch array
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return HEXO_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return HEXO_ERR_CUDA;
+    if (cap != cudaStreamCaptureStatusNone) return HEXO_ERR_UNSUPPORTED;   // the call waits for its results
     unsigned char *base = nullptr;
     uint32_t slots = 0;
     hexo_status st = na_setup(dev, f32, &base, &slots);
     if (st != HEXO_OK) return st;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaSuccess;
     auto up = [&](size_t off, const void *src, size_t bytes) {
         if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(base + off, src, bytes, cudaMemcpyHostToDevice, s);
@@ -272,6 +289,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     up(kOffOpts, od, n_opts * sizeof(OptDesc));
     up(kOffPaths, opt_paths, n_opts * sizeof(uint64_t));
     up(kOffDisc, opt_disc, n_opts * sizeof(double));
+    up(kOffPexp, opt_pexp, n_opts * sizeof(int32_t));
     TileDesc chunk[kNaTileChunk];
     for (uint32_t t0 = 0; t0 < n_tiles && e == cudaSuccess; t0 += kNaTileChunk) {
         const uint32_t cnt = std::min(kNaTileChunk, n_tiles - t0);
@@ -309,7 +327,8 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     double *d_se = reinterpret_cast<double *>(base + kOffSe);
     if (e == cudaSuccess)
         e = launch_finalize(a.acc, 1, a.acc_slot_stride, reinterpret_cast<const uint64_t *>(base + kOffPaths),
-                            reinterpret_cast<const double *>(base + kOffDisc), n_opts, d_price, d_se, nullptr, s);
+                            reinterpret_cast<const double *>(base + kOffDisc),
+                            reinterpret_cast<const int32_t *>(base + kOffPexp), n_opts, d_price, d_se, nullptr, s);
     uint32_t ctl[2] = {0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(price_out, d_price, n_opts * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && stderr_out)

@@ -190,6 +190,7 @@ __device__ __forceinline__ void fold_option(const KernelArgs &a, const SetDesc &
     uint32_t l[kLimbs] = {0, 0, 0, 0, 0, 0};
     bool ok = true, any = false;
     const uint32_t kind = O.kind;
+    const int E = S.pay_exp, eoff = S.pay_exp + 103;   // payoffs in units of 2^E
 #pragma unroll
     for (int p = 0; p < PPT; ++p) {
         if (active[p] && kpath[p] < O.n_paths) {
@@ -198,24 +199,24 @@ __device__ __forceinline__ void fold_option(const KernelArgs &a, const SetDesc &
                 if (kCV && kind == 3u) {
                     const float d = __fsub_rn(fmaxf(0.0f, __fsub_rn(asian[p], K)), fmaxf(0.0f, __fsub_rn(geo[p], K)));
                     any = true;   // every counted path adds its 2^63 bias, zero or not
-                    ok &= dev::limbs_add_signed_f32(d, l);
+                    ok &= dev::limbs_add_signed_f32(d, eoff, l);
                 } else {
                     const float f = kind == 0u ? asian[p] : (kCV && kind == 2u) ? geo[p] : euro[p];
                     const float pay = fmaxf(0.0f, __fsub_rn(f, K));
                     any |= pay != 0.0f;
-                    ok &= dev::limbs_add_f32(pay, l);
+                    ok &= dev::limbs_add_f32(pay, eoff, l);
                 }
             } else {
                 const double K = O.strike;
                 if (kCV && kind == 3u) {
                     const double d = __dsub_rn(fmax(0.0, __dsub_rn(asian[p], K)), fmax(0.0, __dsub_rn(geo[p], K)));
                     any = true;   // every counted path adds its 2^63 bias, zero or not
-                    ok &= dev::limbs_add_signed_f64(d, l);
+                    ok &= dev::limbs_add_signed_f64(d, E, l);
                 } else {
                     const double f = kind == 0u ? asian[p] : (kCV && kind == 2u) ? geo[p] : euro[p];
                     const double pay = fmax(0.0, __dsub_rn(f, K));
                     any |= pay != 0.0;
-                    ok &= dev::limbs_add_f64(pay, l);
+                    ok &= dev::limbs_add_f64(pay, E, l);
                 }
             }
         }
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         for (int p = 0; p < PPT; ++p) {
             kpath[p] = td.path_begin + (uint64_t)p * bd + tid;
             active[p] = kpath[p] < S.n_paths;
-            dev::rng_start<kF32>(g[p], c[p], ring[p], ws[p], S.seed + (uint32_t)kpath[p]);
+            dev::rng_start<kF32>(g[p], c[p], ring[p], ws[p], S.seed + (uint32_t)kpath[p], S.stream);
             pv[p].vd = ds::F2{S.ds_v0[0], S.ds_v0[1]};
             pv[p].lx = kF32 ? (R)(-(float)S.f_r * S.f_v0) : (R)S.logS0;   // FP32: log X - log S0 - (rho/sigma) v
             pv[p].v = kF32 ? (R)S.f_v0 : (R)S.v0;

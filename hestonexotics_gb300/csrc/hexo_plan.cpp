@@ -15,8 +15,8 @@ constexpr uint64_t kMaxPaths = 0xFFFFFFFFull;  // stream seeds are seed + k modu
 }
 
 hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, uint32_t n_opts,
-                     const hexo_mc_cfg &cfg, uint32_t seed, uint64_t path_lo, uint64_t path_hi, SetPlan &out,
-                     std::string &err) {
+                     const hexo_mc_cfg &cfg, uint32_t seed, uint32_t stream, uint64_t path_lo, uint64_t path_hi,
+                     SetPlan &out, std::string &err) {
     out = SetPlan();
     if (n_opts == 0 || opts == nullptr) { err = "request has no options"; return HEXO_ERR_INVALID; }
     const double pv[7] = {p.v0, p.theta, p.rho, p.kappa, p.sigma, p.r, p.q};
@@ -26,7 +26,7 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
         err = "Heston parameters out of range (need v0 >= 0, theta > 0, kappa > 0, sigma > 0, |rho| <= 1)";
         return HEXO_ERR_INVALID;
     }
-    if (!finite(S0) || !(S0 > 0.0)) { err = "S0 must be positive and finite"; return HEXO_ERR_INVALID; }
+    if (!finite(S0) || !(S0 >= 0x1p-60) || !(S0 < 0x1p60)) { err = "S0 must be in [2^-60, 2^60)"; return HEXO_ERR_INVALID; }
     const uint32_t block_words = cfg.rng_block_words ? cfg.rng_block_words : 16u;
     if (block_words != 16u) {
         err = "rng_block_words other than 16 is not supported by the GPU engine";
@@ -176,6 +176,8 @@ hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, u
     sd.f_r = (float)(p.rho / p.sigma);
     ds_split(p.v0, sd.ds_v0);
     sd.seed = seed;
+    sd.stream = stream;
+    sd.pay_exp = pay_exponent(S0);
     sd.seg_count = (uint32_t)out.segs.size();
     sd.mat_count = (uint32_t)m;
     sd.opt_count = (uint32_t)out.opts.size();
@@ -228,6 +230,7 @@ void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_b
         b.n_out = n_out_end;
         b.opt_paths.resize(n_out_end, 0);
         b.opt_disc.resize(n_out_end, 1.0);
+        b.opt_pexp.resize(n_out_end, 0);
     }
     for (size_t i = 0; i < sp.opts.size(); ++i) {
         const uint32_t o = global(sp.opts[i].out_index);
@@ -235,6 +238,7 @@ void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_b
         const uint64_t hi = std::min<uint64_t>(sp.opts[i].n_paths, sp.path_hi);
         b.opt_paths[o] = hi > sp.path_lo ? hi - sp.path_lo : 0;
         b.opt_disc[o] = sp.opt_disc[i];
+        b.opt_pexp[o] = sp.set.pay_exp;
     }
     b.max_mats = std::max<uint32_t>(b.max_mats, (uint32_t)sp.mats.size());
     b.set_params.push_back(sp.params);
@@ -284,8 +288,8 @@ void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans) {
     for (const Costed &c : all) b.tiles.push_back(c.t);
 }
 
-void finalize_one(const uint64_t *limbs, uint64_t n_paths, double disc, double *price, double *se) {
-    finalize_limbs6(limbs, n_paths, disc, price, se);
+void finalize_one(const uint64_t *limbs, uint64_t n_paths, double disc, int pay_exp, double *price, double *se) {
+    finalize_limbs6(limbs, n_paths, disc, pay_exp, price, se);
 }
 
 } // namespace hexo

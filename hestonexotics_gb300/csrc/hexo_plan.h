@@ -36,7 +36,7 @@ struct SetPlan {
 
 // Validates and plans one request.  Returns HEXO_OK or an error with a message.
 hexo_status plan_set(const hexo_params &p, double S0, const hexo_option *opts, uint32_t n_opts,
-                     const hexo_mc_cfg &cfg, uint32_t seed, uint64_t path_lo, uint64_t path_hi,
+                     const hexo_mc_cfg &cfg, uint32_t seed, uint32_t stream, uint64_t path_lo, uint64_t path_hi,
                      SetPlan &out, std::string &err);
 
 // Last maturity index a path k needs, or -1 when no option uses path k.
@@ -55,6 +55,7 @@ struct BatchPlan {
     std::vector<TileDesc> tiles;
     std::vector<uint64_t> opt_paths;    // per output slot: paths that price it
     std::vector<double> opt_disc;       // per output slot: exp(-r T)
+    std::vector<int32_t> opt_pexp;      // per output slot: E, payoffs summed in units of 2^E
     uint32_t n_out = 0;                 // output slots: the requests' options, then the control variate's
     std::vector<hexo_params> set_params;
     struct CvLeader {                   // an Asian option priced with the geometric control variate
@@ -76,6 +77,6 @@ void batch_tiles(BatchPlan &b, const std::vector<SetPlan> &plans);
 
 // Finaliser arithmetic shared bit for bit with the device finaliser:
 // price and standard error from six limb sums.
-void finalize_one(const uint64_t *limbs, uint64_t n_paths, double disc, double *price, double *se);
+void finalize_one(const uint64_t *limbs, uint64_t n_paths, double disc, int pay_exp, double *price, double *se);
 
 } // namespace hexo

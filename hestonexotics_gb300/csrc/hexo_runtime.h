@@ -47,6 +47,7 @@ struct DeviceBatch {
     KernelArgs args{};
     uint64_t *d_paths = nullptr;
     double *d_disc = nullptr, *d_price = nullptr, *d_se = nullptr;
+    int32_t *d_pexp = nullptr;       // per output slot: E, payoffs summed in units of 2^E
     double *h_price = nullptr, *h_se = nullptr;
     unsigned long long *h_acc = nullptr;
     double *d_cv_eg = nullptr;         // control variate: E[(G - K)^+] per output slot (NaN elsewhere)

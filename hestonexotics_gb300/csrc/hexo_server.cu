@@ -170,8 +170,8 @@ bool launch_next(hexo_server *s, std::unique_lock<std::mutex> &lk) {
         SrvReq *r = s->pending.front();
         if (!r->planned) {
             std::string err;
-            r->status = plan_set(r->req.params, r->req.S0, r->req.opts, r->req.n_opts, s->opts.cfg, r->req.seed, 0,
-                                 ~0ull, r->plan, err);
+            r->status = plan_set(r->req.params, r->req.S0, r->req.opts, r->req.n_opts, s->opts.cfg, r->req.seed,
+                                 r->req.stream, 0, ~0ull, r->plan, err);
             r->planned = true;
             if (r->status != HEXO_OK) {
                 s->pending.pop_front();

@@ -11,12 +11,29 @@
 // (set, path block) work items for the persistent kernel.
 #pragma once
 #include <stdint.h>
+#include <math.h>
 
 namespace hexo {
 
-constexpr int kLimbs = 6;            // 3 x 25-bit limbs of sum(pay*2^40), 3 of sum(pay^2*2^24)
+// Fixed-point payoff sums.  A request's payoffs are measured in units of
+// 2^E, E the binary exponent of its spot (2^(E-1) <= S0 < 2^E): y = pay 2^-E
+// is of order one whatever the spot, so the sums keep the same relative
+// precision at S0 = 1e-3 as at 1e8.  Per path q = round(y 2^47) and
+// q2 = round(y^2 2^43) (ties to even), y < 2^16, so q < 2^63 and q2 < 2^75,
+// each cut into three 25-bit limbs.
+constexpr int kLimbs = 6;            // 3 x 25-bit limbs of sum(q), 3 of sum(q2)
 constexpr int kLimbBits = 25;        // a warp adds up to 128 limb values in 32 bits
 constexpr uint32_t kLimbMask = (1u << kLimbBits) - 1u;
+constexpr int kPayFrac = 47;         // q = round(y 2^47)
+constexpr int kSqFrac = 43;          // q2 = round(y^2 2^43)
+constexpr int kPayExpMin = -59, kPayExpMax = 60;   // spots in [2^-60, 2^60)
+
+// E of a spot (the exponent frexp returns); callers check the range.
+inline int pay_exponent(double S0) {
+    int e = 0;
+    (void)frexp(S0, &e);
+    return e;
+}
 constexpr int kRngWords = 16;        // words per RNG buffer (one SHISHUA block)
 constexpr uint32_t kConvQueue = 96;                    // per warp: queued conversion items
 constexpr uint32_t kWarpScratchBytes = kConvQueue * 2; // per warp: the queue
@@ -68,7 +85,8 @@ struct SetDesc {
     double S0, logS0, v0, theta;
     float f_S0, f_v0, f_theta, f_r;   // f_r = rho / sigma
     float ds_v0[2];                   // v0 in double-single (FP32 form)
-    float f_pad1[2];
+    uint32_t stream;                  // seed word 1 of every path's SHISHUA stream
+    int32_t pay_exp;                  // E: payoffs are summed in units of 2^E
     uint32_t seed;
     uint32_t seg_begin, seg_count;
     uint32_t mat_begin, mat_count;

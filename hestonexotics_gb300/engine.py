@@ -53,11 +53,12 @@ class Config:
     paths_per_thread: int = 0
     unroll: int = 0
     control_variate: int = 0   # 1: Asian options with the geometric-average control variate
+    stream: int = 0            # seed word 1 of the paths' streams (hexo_price, partial, no-allocation)
 
     def c(self) -> L.hexo_mc_cfg:
         return L.hexo_mc_cfg(self.n_paths, self.step_mode, self.steps, self.steps_per_year, self.seed & 0xFFFFFFFF,
                              self.rng_block_words, self.precision, self.block, self.paths_per_thread, self.unroll,
-                             self.control_variate, 0)
+                             self.control_variate, self.stream & 0xFFFFFFFF)
 
 
 @dataclass
@@ -94,10 +95,14 @@ class Options:
 
 @dataclass
 class Request:
+    """One pricing request.  Path k draws from the SHISHUA stream seeded
+    {seed + k, stream, 0, 0}: give the requests of one batch or one server
+    different stream numbers so that no two share a path's stream."""
     params: Params
     S0: float
     options: Options
     seed: int = 42
+    stream: int = 0
 
 
 def _dp(a: np.ndarray):
@@ -316,6 +321,7 @@ class Engine:
             arr[i].opts = C.cast(opts, C.POINTER(L.hexo_option))
             arr[i].n_opts = n
             arr[i].seed = int(rq.seed) & 0xFFFFFFFF
+            arr[i].stream = int(rq.stream) & 0xFFFFFFFF
             arr[i].price_out = _dp(price)
             arr[i].stderr_out = _dp(se)
         keep.append(arr)
@@ -407,15 +413,16 @@ class Engine:
                 "best_ms": res.best_ms, "table": table}
 
     # --------------------------------------------------------------- debug
-    def rng_words(self, seed: int, n_streams: int, n_words: int) -> np.ndarray:
+    def rng_words(self, seed: int, n_streams: int, n_words: int, stream: int = 0) -> np.ndarray:
         out = np.zeros(n_streams * n_words, dtype=np.uint64)
-        self._check(self._lib.hexo_debug_rng_words(self._ctx, seed & 0xFFFFFFFF, n_streams, n_words, _u64p(out)))
+        self._check(self._lib.hexo_debug_rng_words(self._ctx, seed & 0xFFFFFFFF, stream & 0xFFFFFFFF, n_streams,
+                                                   n_words, _u64p(out)))
         return out.reshape(n_streams, n_words)
 
-    def rng_draws(self, seed: int, n_streams: int, kinds: np.ndarray) -> np.ndarray:
+    def rng_draws(self, seed: int, n_streams: int, kinds: np.ndarray, stream: int = 0) -> np.ndarray:
         kinds = np.ascontiguousarray(kinds, dtype=np.uint8)
         out = np.zeros(n_streams * len(kinds))
-        self._check(self._lib.hexo_debug_rng_draws(self._ctx, seed & 0xFFFFFFFF, n_streams,
+        self._check(self._lib.hexo_debug_rng_draws(self._ctx, seed & 0xFFFFFFFF, stream & 0xFFFFFFFF, n_streams,
                                                    kinds.ctypes.data_as(C.POINTER(C.c_uint8)), len(kinds), _dp(out)))
         return out.reshape(n_streams, len(kinds))
 
@@ -425,11 +432,12 @@ class Engine:
         self._check(self._lib.hexo_debug_normals(self._ctx, _u64p(words), len(words), _dp(out)))
         return out
 
-    def payoff_limbs(self, pay: np.ndarray, precision: int) -> np.ndarray:
-        """The kernels' 25-bit limbs of round(pay 2^40) and round(pay^2 2^24), [n, 6]."""
+    def payoff_limbs(self, pay: np.ndarray, precision: int, S0: float = 100.0) -> np.ndarray:
+        """The kernels' 25-bit limbs of round(y 2^47) and round(y^2 2^43), y = pay 2^-E with
+        2^(E-1) <= S0 < 2^E, [n, 6]."""
         pay = np.ascontiguousarray(pay, dtype=np.float64)
         out = np.zeros(len(pay) * 6, dtype=np.uint32)
-        self._check(self._lib.hexo_debug_payoff_limbs(self._ctx, _dp(pay), len(pay), precision,
+        self._check(self._lib.hexo_debug_payoff_limbs(self._ctx, _dp(pay), len(pay), precision, float(S0),
                                                       out.ctypes.data_as(C.POINTER(C.c_uint32))))
         return out.reshape(len(pay), 6)
 
@@ -464,8 +472,9 @@ def swift_params_dynamic(params: Params, tau: float, S: float, K_min: float, K_m
     return {k: getattr(out, k) for k in ("m", "exp2_m", "sqrt_exp2_m", "lower", "upper", "k1", "k2", "J")}
 
 
-def finalize_limbs(params: Params, options: Options, cfg: Config, limbs: np.ndarray):
-    """Host-only finalisation of (merged) limb sums; bit-identical to the device finaliser."""
+def finalize_limbs(params: Params, S0: float, options: Options, cfg: Config, limbs: np.ndarray):
+    """Host-only finalisation of (merged) limb sums of a request with spot S0;
+    bit-identical to the device finaliser."""
     lib = L.load()
     n = len(options)
     limbs = np.ascontiguousarray(limbs, dtype=np.uint64).reshape(-1)
@@ -473,7 +482,8 @@ def finalize_limbs(params: Params, options: Options, cfg: Config, limbs: np.ndar
     se = np.zeros(n)
     p = params.c()
     c = cfg.c()
-    st = lib.hexo_finalize_limbs(C.byref(p), options.c_array(), n, C.byref(c), _u64p(limbs), _dp(price), _dp(se))
+    st = lib.hexo_finalize_limbs(C.byref(p), float(S0), options.c_array(), n, C.byref(c), _u64p(limbs), _dp(price),
+                                 _dp(se))
     if st != L.HEXO_OK:
         raise L.HexoError(st, "hexo_finalize_limbs")
     return price, se

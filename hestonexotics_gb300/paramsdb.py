@@ -53,8 +53,8 @@ class ParamsDB:
         return [r[0] for r in self._db.execute("SELECT Name FROM HestonParameters ORDER BY Name")]
 
     def request(self, name: str, S0: float, options: Options, seed: int = 42, r: float = 0.0,
-                q: float = 0.0) -> Request:
-        return Request(self.fetch(name, r, q), S0, options, seed)
+                q: float = 0.0, stream: int = 0) -> Request:
+        return Request(self.fetch(name, r, q), S0, options, seed, stream)
 
     def close(self) -> None:
         self._db.close()

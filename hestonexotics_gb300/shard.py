@@ -73,7 +73,7 @@ def price_sharded(request: E.Request, cfg: E.Config, *, rank: int | None = None,
     lo, hi = shard_range(max_paths(request, cfg), rank, world)
     limbs = np.ascontiguousarray(partial(request, cfg, lo, hi), dtype=np.uint64).reshape(len(request.options), 6)
     total = _all_reduce_sum(limbs, group)
-    return E.finalize_limbs(request.params, request.options, cfg, total)
+    return E.finalize_limbs(request.params, request.S0, request.options, cfg, total)
 
 
 def price_batch_sharded(requests: Sequence[E.Request], cfg: E.Config, **kw):

@@ -18,6 +18,10 @@ path counts.
                      Asian:European 3:1
   request_stream()   Poisson arrivals (seed 3) of single-set requests with
                      1-400 options and target-SE path counts
+
+Every request of a batch or of a request stream gets its own stream number
+(seed word 1 of its paths' generators), so no two requests share a path's
+random stream even where their seed ranges [seed, seed + paths) overlap.
 """
 from __future__ import annotations
 
@@ -96,7 +100,7 @@ def uneven_batch(n_sets: int = 64, seed: int = 2, precision: int = FP32, path_sc
         paths_u = np.maximum(1, np.rint(paths_u * path_scale)).astype(np.uint64)
         n_paths = paths_u[np.searchsorted(uT, T)]
         reqs.append(Request(params, S0_DEFAULT, Options(strike=K, T=T, payoff=kind, n_paths=n_paths),
-                            seed=int(rng.integers(0, 2 ** 32))))
+                            seed=int(rng.integers(0, 2 ** 32)), stream=s))
     cfg = Config(n_paths=1 << 14, step_mode=STEP_GRID, steps_per_year=252.0, seed=seed, precision=precision)
     return reqs, cfg
 
@@ -131,6 +135,30 @@ def request_stream(rate_per_s: float, duration_s: float, seed: int = 3, max_opts
         kind = np.where(rng.random(n) < 0.75, ASIAN, EUROPEAN).astype(np.uint32)
         npaths = target_paths(S0_DEFAULT)
         out.append(Arrival(t, Request(params, S0_DEFAULT, Options(strike=K, T=T, payoff=kind, n_paths=npaths),
-                                      seed=int(rng.integers(0, 2 ** 32)))))
+                                      seed=int(rng.integers(0, 2 ** 32)), stream=len(out))))
     cfg = Config(n_paths=1 << 14, step_mode=STEP_GRID, steps_per_year=252.0, seed=seed, precision=FP32)
     return out, cfg
+
+
+def stream_overlaps(requests, n_default: int = 1 << 14):
+    """Pairs (i, j, paths) of requests whose paths share SHISHUA streams: the
+    same stream number and overlapping seed ranges [seed, seed + n) modulo
+    2^32, n the request's largest path count.  Empty for the workloads here."""
+    spans = []
+    for i, rq in enumerate(requests):
+        n = rq.options.n_paths.astype(np.uint64)
+        n = int(np.where(n == 0, np.uint64(n_default), n).max())
+        spans.append((int(rq.stream) & 0xFFFFFFFF, int(rq.seed) & 0xFFFFFFFF, n, i))
+    out = []
+    by_stream = {}
+    for st, seed, n, i in spans:
+        by_stream.setdefault(st, []).append((seed, n, i))
+    for group in by_stream.values():
+        for a in range(len(group)):
+            for b in range(a + 1, len(group)):
+                (sa, na, ia), (sb, nb, ib) = group[a], group[b]
+                d = (sb - sa) % (1 << 32)            # b's first seed as an offset into a's range
+                shared = max(0, min(na, d + nb) - d) + max(0, min(nb, (1 << 32) - d + na) - ((1 << 32) - d))
+                if shared:
+                    out.append((ia, ib, shared))
+    return out

@@ -18,15 +18,28 @@
  * hexo_ctx_last_error().  include/hexo/reference_compat.h wraps this ABI
  * in the reference's own C++ signature.
  *
- * Random numbers.  Path k (0-based) of a request draws from its own stream,
- * exactly the reference RNG class (src/inc/RNG.h:17-52, src/RNG.cpp:8-47)
- * constructed as RNG(rng_block_words, (uint32_t)(seed + k)): one SHISHUA
- * stream seeded {seed + k, 0, 0, 0} filling a uniform buffer first and a
- * normal buffer next, each refilled from the same stream when it runs dry;
+ * Random numbers.  Path k (0-based) of a request draws from its own SHISHUA
+ * stream seeded {(uint32_t)(seed + k), stream, 0, 0}, used exactly as the
+ * reference RNG class uses its stream (src/inc/RNG.h:17-52,
+ * src/RNG.cpp:8-47): a uniform buffer filled first and a normal buffer next,
+ * each refilled from the same stream when it runs dry;
  * u = (double)word / (double)UINT64_MAX; normals are the float32 AS241
- * (reference src/as241.f90).  Results therefore do not depend on block
- * size, paths per thread, batching, sharding or which other requests share
- * a launch.
+ * (reference src/as241.f90).  With stream = 0 this is the reference class
+ * RNG(rng_block_words, seed + k) itself; the second seed word (the
+ * reference's seed is four words, RNG.h:24) separates requests, so requests
+ * with different stream numbers never share a path's stream even when their
+ * seed ranges [seed, seed + n_paths) overlap.  Results do not depend on
+ * block size, paths per thread, batching, sharding or which other requests
+ * share a launch.
+ *
+ * Payoff sums.  Prices and standard errors come from exact integer sums, so
+ * they are bit for bit the same however paths are split across CTAs,
+ * launches or devices.  A request's payoffs are summed in units of 2^E, E the
+ * binary exponent of its spot (2^(E-1) <= S0 < 2^E): per path
+ * q = round(y 2^47) and q2 = round(y^2 2^43) with y = pay 2^-E, so prices and
+ * standard errors keep the same relative precision at every spot level.
+ * Spots must lie in [2^-60, 2^60); a payoff at or above 2^16 2^E (65,536
+ * times the spot or more) returns HEXO_ERR_NUMERIC.
  */
 #ifndef HEXO_MC_H
 #define HEXO_MC_H
@@ -41,8 +54,11 @@ extern "C" {
 /* Raised whenever a struct's layout or a function's signature changes.
  * 2: hexo_batch_info.quad_steps; hexo_debug_pipe_peaks fills five rates;
  *    hexo_debug_payoff_limbs.
- * 3: hexo_mc_cfg.control_variate. */
-#define HEXO_ABI_VERSION 3u
+ * 3: hexo_mc_cfg.control_variate.
+ * 4: the stream seed word (hexo_mc_cfg.stream, hexo_request.stream); limb
+ *    sums in units of the spot's power of two (hexo_finalize_limbs and
+ *    hexo_debug_payoff_limbs take S0); the debug RNG calls take the stream. */
+#define HEXO_ABI_VERSION 4u
 
 typedef enum hexo_status {
     HEXO_OK = 0,
@@ -139,11 +155,12 @@ typedef struct hexo_mc_cfg {
                                  comes from the Heston characteristic function, and beta is
                                  estimated from the paths; Europeans unchanged.  Not with
                                  hexo_price_partial or hexo_price_noalloc. */
-    uint32_t reserved;
+    uint32_t stream;          /* seed word 1 of every path's stream for hexo_price, hexo_price_partial,
+                                 hexo_price_noalloc; 0 = the reference's RNG(16, seed + k) */
 } hexo_mc_cfg;
 
 /* Fills cfg with the defaults: 65,536 paths, REFERENCE stepping with 252
- * steps, seed 42, 16-word RNG buffers, FP64, tuned launch shape. */
+ * steps, seed 42, stream 0, 16-word RNG buffers, FP64, tuned launch shape. */
 void hexo_mc_cfg_default(hexo_mc_cfg *cfg);
 
 /* ------------------------------------------------------- plain pricing */
@@ -164,6 +181,9 @@ typedef struct hexo_request {
     uint32_t seed;
     double *price_out;   /* n_opts */
     double *stderr_out;  /* n_opts, may be NULL */
+    uint32_t stream;     /* seed word 1 of this request's paths; give the requests of one batch or one
+                            server different numbers so that none shares a path's stream */
+    uint32_t reserved;   /* 0 */
 } hexo_request;
 
 /* Prices many parameter sets in one persistent launch. */
@@ -313,17 +333,18 @@ hexo_status hexo_calib_destroy(hexo_calib *c);
 /* --------------------------------------------------------------- shards */
 
 /* Exact partial sums over paths [path_lo, path_hi) of one request: for each
- * option six uint64 limbs (sum round(pay*2^40) and sum round(pay^2*2^24),
- * each split into three 25-bit limb sums).  Limb sums of disjoint path
- * ranges add exactly, so any split across shards or devices merges to the
- * bit-identical result of one launch. */
+ * option six uint64 limbs, the sums of q = round(y 2^47) and of
+ * q2 = round(y^2 2^43) with y = pay 2^-E (2^(E-1) <= S0 < 2^E), each split
+ * into three 25-bit limb sums.  Limb sums of disjoint path ranges add
+ * exactly, so any split across shards or devices merges to the bit-identical
+ * result of one launch. */
 #define HEXO_LIMBS 6
 hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, const hexo_option *opts,
                                uint32_t n_opts, const hexo_mc_cfg *cfg, uint64_t path_lo, uint64_t path_hi,
                                uint64_t *limbs_out /* n_opts * HEXO_LIMBS */);
 /* Host-only: prices and standard errors from (merged) limb sums; the same
  * operation sequence as the device finaliser, so results match it bit for bit. */
-hexo_status hexo_finalize_limbs(const hexo_params *p, const hexo_option *opts, uint32_t n_opts,
+hexo_status hexo_finalize_limbs(const hexo_params *p, double S0, const hexo_option *opts, uint32_t n_opts,
                                 const hexo_mc_cfg *cfg, const uint64_t *limbs, double *price_out,
                                 double *stderr_out);
 
@@ -396,22 +417,25 @@ hexo_status hexo_autotune(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_re
 
 /* ---------------------------------------------------------------- debug */
 
-/* Raw SHISHUA words of streams seed+k, k in [0, n_streams): out[k*n_words + i]. */
-hexo_status hexo_debug_rng_words(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, uint32_t n_words,
-                                 uint64_t *out);
-/* Draws of RNG(16, seed + k) for n_streams streams following one shared
+/* Raw SHISHUA words of the streams seeded {seed + k, stream, 0, 0}, k in
+ * [0, n_streams): out[k*n_words + i]. */
+hexo_status hexo_debug_rng_words(hexo_ctx *ctx, uint32_t seed, uint32_t stream, uint32_t n_streams,
+                                 uint32_t n_words, uint64_t *out);
+/* Draws of the two-buffer RNG on the streams seeded {seed + k, stream, 0, 0}
+ * (stream 0: RNG(16, seed + k)) for n_streams streams following one shared
  * kinds[] sequence (0 = normal, 1 = uniform); out[k*n + i]. */
-hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t n_streams, const uint8_t *kinds,
-                                 uint32_t n, double *out);
+hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t stream, uint32_t n_streams,
+                                 const uint8_t *kinds, uint32_t n, double *out);
 /* AS241 of u = (double)w / (double)UINT64_MAX for each word: out[i]. */
 hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n, double *out);
-/* The fixed-point split of payoffs as the path kernels fold them: for each
- * pay[i] (converted to float first when precision is HEXO_FP32) the six
- * 25-bit limbs out[6*i .. 6*i+5] of q = round(pay * 2^40) and
- * q2 = round(pay^2 * 2^24), ties to even (pay^2 rounded to double in the
- * FP64 form, exact in the FP32 form); all six are 0xFFFFFFFF for a payoff
- * the kernels reject (not finite, negative or >= 2^23). */
-hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision,
+/* The fixed-point split of payoffs as the path kernels fold them for a
+ * request with spot S0: for each pay[i] (converted to float first when
+ * precision is HEXO_FP32) the six 25-bit limbs out[6*i .. 6*i+5] of
+ * q = round(y 2^47) and q2 = round(y^2 2^43), y = pay 2^-E,
+ * 2^(E-1) <= S0 < 2^E, ties to even (y^2 rounded to double in the FP64 form,
+ * exact in the FP32 form); all six are 0xFFFFFFFF for a payoff the kernels
+ * reject (not finite, negative or y >= 2^16). */
+hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision, double S0,
                                     uint32_t *out);
 /* Measured lane-operation rates (per second) of this GPU's pipes, from
  * throughput probes: out5 = {FP32 FMA, FP64 FMA, MUFU ex2, INT32 IMAD,

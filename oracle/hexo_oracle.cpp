@@ -8,7 +8,10 @@
  *
  * What it restates (reference file:line):
  *   OracleRNG        RNG wrapper, src/inc/RNG.h:17-52 + src/RNG.cpp:8-47:
- *                    one SHISHUA stream seeded {seed,0,0,0} feeds a uniform
+ *                    one SHISHUA stream seeded {seed,0,0,0} (the engine's
+ *                    per-request stream number goes to seed word 1, which
+ *                    the reference's four-word seed, RNG.h:24, leaves 0)
+ *                    feeds a uniform
  *                    buffer (filled first) and a normal buffer (filled next);
  *                    each refills from the same stream when it runs dry;
  *                    u = (double)w / (double)UINT64_MAX (RNG.cpp:31); normals
@@ -27,7 +30,8 @@
  *                    accumulation `prices[i] += payoff/n` (tpp:40) kept in
  *                    path order but race-free (per-thread arrays).
  *   per-path driver: the stream partition the GPU engine uses: path k of a
- *                    request draws from its own RNG(block_words, seed+k);
+ *                    request draws from its own RNG(block_words, seed+k),
+ *                    seeded {seed+k, stream, 0, 0};
  *                    oracle_branch_counts walks the same paths and counts
  *                    the QE steps on the quadratic branch (tpp:63-68).
  *
@@ -75,8 +79,8 @@ class OracleRNG {
     }
 
 public:
-    OracleRNG(size_t size, uint64_t seed0) : u_(size), g_(size), cu_(0), cg_(0), size_(size) {
-        uint64_t seed[4] = {seed0, 0, 0, 0};
+    OracleRNG(size_t size, uint64_t seed0, uint64_t seed1 = 0) : u_(size), g_(size), cu_(0), cg_(0), size_(size) {
+        uint64_t seed[4] = {seed0, seed1, 0, 0};
         prng_init(&s_, seed);
         fill_uniform(u_);
         fill_normal();
@@ -197,15 +201,26 @@ inline double payoff_of(const Problem &pr, uint32_t o, double asian, double euro
     return std::max(0., fv - pr.strike[o]);                             // AsianContract.h:43-47
 }
 
-/* Exact fixed-point accumulation in the engine's format: q = round(pay*2^40)
- * and q2 = round(pay^2*2^24) (ties to even), each split into three 25-bit
- * limbs; limb sums are exact, so the order of paths does not matter. */
+/* The binary exponent E of a spot, 2^(E-1) <= S0 < 2^E: payoffs are summed
+ * in units of 2^E. */
+inline int pay_exponent(double S0) {
+    int e = 0;
+    (void)std::frexp(S0, &e);
+    return e;
+}
+
+/* Exact fixed-point accumulation in the engine's format: with y = pay 2^-E,
+ * q = round(y*2^47) and q2 = round(y^2*2^43) (y^2 rounded to double, ties to
+ * even), each split into three 25-bit limbs; limb sums are exact, so the
+ * order of paths does not matter. */
 struct ExactSums {
     std::vector<uint64_t> l;   // [o*6 + limb]
-    explicit ExactSums(size_t n) : l(6 * n, 0) {}
+    int E;
+    ExactSums(size_t n, int E_) : l(6 * n, 0), E(E_) {}
     void add(uint32_t o, double pay) {
-        const unsigned __int128 q = (unsigned __int128)std::nearbyint(pay * 0x1p40);
-        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(pay * pay * 0x1p24);
+        const double y = std::ldexp(pay, -E);
+        const unsigned __int128 q = (unsigned __int128)std::nearbyint(y * 0x1p47);
+        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(y * y * 0x1p43);
         const uint64_t M = (1ull << 25) - 1;
         uint64_t *d = &l[6 * (size_t)o];
         d[0] += (uint64_t)(q & M); d[1] += (uint64_t)((q >> 25) & M); d[2] += (uint64_t)(q >> 50);
@@ -380,15 +395,18 @@ void cv_geo_calls(const Params &p, double S0, const std::vector<double> &dts, co
     if (F_out) *F_out = F;
 }
 
-/* Signed fixed-point sums of the control variate's differences: q + 2^63
- * (q = round(d 2^40)) and q2 = round(d^2 2^24), three 25-bit limbs each. */
+/* Signed fixed-point sums of the control variate's differences, with
+ * y = d 2^-E: q + 2^63 (q = round(y 2^47)) and q2 = round(y^2 2^43), three
+ * 25-bit limbs each. */
 struct SignedSums {
     std::vector<uint64_t> l;
-    explicit SignedSums(size_t n) : l(6 * n, 0) {}
+    int E;
+    SignedSums(size_t n, int E_) : l(6 * n, 0), E(E_) {}
     void add(uint32_t o, double d) {
-        const __int128 q = (__int128)std::nearbyint(d * 0x1p40);
+        const double y = std::ldexp(d, -E);
+        const __int128 q = (__int128)std::nearbyint(y * 0x1p47);
         const unsigned __int128 qu = (unsigned __int128)(q + ((__int128)1 << 63));
-        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(d * d * 0x1p24);
+        const unsigned __int128 q2 = (unsigned __int128)std::nearbyint(y * y * 0x1p43);
         const uint64_t M = (1ull << 25) - 1;
         uint64_t *dd = &l[6 * (size_t)o];
         dd[0] += (uint64_t)(qu & M); dd[1] += (uint64_t)((qu >> 25) & M); dd[2] += (uint64_t)(qu >> 50);
@@ -412,9 +430,11 @@ void oracle_shishua_words(const uint64_t seed4[4], uint64_t n_words, uint64_t *o
     }
 }
 
-/* Draws of RNG(block_words, seed): kinds[i] = 0 -> get_grand, 1 -> get_urand. */
-void oracle_rng_draws(uint32_t seed, uint32_t block_words, const uint8_t *kinds, uint64_t n, double *out) {
-    OracleRNG rng(block_words, seed);
+/* Draws of RNG(block_words, seed) on the stream seeded {seed, stream, 0, 0}:
+ * kinds[i] = 0 -> get_grand, 1 -> get_urand. */
+void oracle_rng_draws(uint32_t seed, uint32_t stream, uint32_t block_words, const uint8_t *kinds, uint64_t n,
+                      double *out) {
+    OracleRNG rng(block_words, seed, stream);
     for (uint64_t i = 0; i < n; ++i) out[i] = kinds[i] ? rng.urand() : rng.grand();
 }
 
@@ -432,17 +452,18 @@ float oracle_logf_c(float x) { return oracle_logf(x); }
 
 /*
  * Per-path stream partition (the GPU engine's): path k uses
- * RNG(block_words, (uint32)(seed + k)); option o is priced on paths
- * k < n_paths[o].  Outputs per option, over paths [path_lo, path_hi):
- * discounted price, its standard error, and six limb sums (the engine's
- * format: 25-bit limbs of round(pay*2^40) and round(pay^2*2^24)).
+ * RNG(block_words, (uint32)(seed + k)) on the stream seeded
+ * {seed + k, stream, 0, 0}; option o is priced on paths k < n_paths[o].
+ * Outputs per option, over paths [path_lo, path_hi): discounted price, its
+ * standard error, and six limb sums (the engine's format: 25-bit limbs of
+ * round(y*2^47) and round(y^2*2^43), y = pay 2^-E, 2^(E-1) <= S0 < 2^E).
  * params7 = {v0, theta(v_m), rho, kappa, sigma, r, q}; HParams order,
  * src/inc/HDistribution.h:9-24.  step_mode 0 = the reference's T_i/steps
  * stepping; 1 = max(5, round(steps_per_year*T_i)) steps per maturity.
  */
 int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
                        const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
-                       double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                       double steps_per_year, uint32_t seed, uint32_t stream, uint32_t block_words, uint64_t path_lo,
                        uint64_t path_hi, int n_threads, double *price, double *stderr_out, uint64_t *limbs_out) {
     Problem pr;
     int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
@@ -455,7 +476,8 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
     uint64_t n_max = *std::max_element(mat_paths.begin(), mat_paths.end());
     path_hi = std::min(path_hi, n_max);
     int nt = n_threads > 0 ? n_threads : 1;
-    std::vector<ExactSums> part(nt, ExactSums(n_opts));
+    const int E = pay_exponent(S0);
+    std::vector<ExactSums> part(nt, ExactSums(n_opts, E));
 #pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
     for (int64_t k = (int64_t)path_lo; k < (int64_t)path_hi; ++k) {
 #ifdef _OPENMP
@@ -466,7 +488,7 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
         size_t last = 0;
         for (size_t j = 0; j < pr.T.size(); ++j)
             if (mat_paths[j] > (uint64_t)k) last = j;
-        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k), stream);
         run_path(pr, rng, false, [&](size_t j, double asian, double euro, double) {
             for (uint32_t o : pr.opts[j])
                 if ((uint64_t)k < n_paths[o]) acc.add(o, payoff_of(pr, o, asian, euro));
@@ -480,8 +502,8 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
         const unsigned __int128 s1 = ExactSums::value(d), s2 = ExactSums::value(d + 3);
         const uint64_t hi = std::min<uint64_t>(n_paths[o], path_hi);
         const double n = hi > path_lo ? (double)(hi - path_lo) : 0.0;
-        const long double mean = n > 0 ? ((long double)s1 / 0x1p40L) / n : 0.L;
-        const long double m2 = n > 0 ? ((long double)s2 / 0x1p24L) / n : 0.L;
+        const long double mean = n > 0 ? std::ldexp((long double)s1, E - 47) / n : 0.L;
+        const long double m2 = n > 0 ? std::ldexp((long double)s2, 2 * E - 43) / n : 0.L;
         long double var = n > 1 ? (m2 - mean * mean) * n / (n - 1) : 0.L;
         if (var < 0) var = 0;
         const double disc = std::exp(-pr.p.r * T[o]);
@@ -500,8 +522,8 @@ int oracle_price_paths(const double *params7, double S0, uint32_t n_opts, const 
  */
 int oracle_branch_counts(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
                          const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
-                         double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
-                         uint64_t path_hi, int n_threads, uint64_t *counts) {
+                         double steps_per_year, uint32_t seed, uint32_t stream, uint32_t block_words,
+                         uint64_t path_lo, uint64_t path_hi, int n_threads, uint64_t *counts) {
     Problem pr;
     int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
     if (rc) return rc;
@@ -523,7 +545,7 @@ int oracle_branch_counts(const double *params7, double S0, uint32_t n_opts, cons
         size_t last = 0;
         for (size_t j = 0; j < pr.T.size(); ++j)
             if (mat_paths[j] > (uint64_t)k) last = j;
-        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k), stream);
         run_path(pr, rng, false, [&](size_t j, double, double, double) { return j < last; }, c);
     }
     counts[0] = counts[1] = 0;
@@ -539,7 +561,7 @@ int oracle_branch_counts(const double *params7, double S0, uint32_t n_opts, cons
  */
 int oracle_path_finals(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
                        const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
-                       double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
+                       double steps_per_year, uint32_t seed, uint32_t stream, uint32_t block_words, uint64_t path_lo,
                        uint64_t path_hi, double *asian_out, double *euro_out, uint32_t *n_mats_out) {
     Problem pr;
     int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
@@ -559,7 +581,7 @@ int oracle_path_finals(const double *params7, double S0, uint32_t n_opts, const 
             euro_out[(k - path_lo) * m + j] = NAN;
         }
         if (!any) continue;
-        OracleRNG rng(block_words, static_cast<uint32_t>(seed + k));
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + k), stream);
         run_path(pr, rng, false, [&](size_t j, double asian, double euro, double) {
             asian_out[(k - path_lo) * m + j] = asian;
             euro_out[(k - path_lo) * m + j] = euro;
@@ -638,8 +660,8 @@ int oracle_geo_calls(const double *params7, double S0, uint32_t n_opts, const do
  */
 int oracle_price_paths_cv(const double *params7, double S0, uint32_t n_opts, const double *strike, const double *T,
                           const uint8_t *kind, const uint64_t *n_paths, uint32_t step_mode, uint32_t steps,
-                          double steps_per_year, uint32_t seed, uint32_t block_words, uint64_t path_lo,
-                          uint64_t path_hi, int n_threads, double *price, double *stderr_out) {
+                          double steps_per_year, uint32_t seed, uint32_t stream, uint32_t block_words,
+                          uint64_t path_lo, uint64_t path_hi, int n_threads, double *price, double *stderr_out) {
     Problem pr;
     int rc = build_problem(pr, params7, S0, n_opts, strike, T, kind, n_paths, step_mode, steps, steps_per_year);
     if (rc) return rc;
@@ -654,8 +676,9 @@ int oracle_price_paths_cv(const double *params7, double S0, uint32_t n_opts, con
     path_hi = std::min(path_hi, n_max);
     const int nt = n_threads > 0 ? n_threads : 1;
     // per thread: a sums (ExactSums [o]), g sums (ExactSums [o]), d sums (SignedSums [o])
-    std::vector<ExactSums> pa(nt, ExactSums(n_opts)), pg(nt, ExactSums(n_opts));
-    std::vector<SignedSums> pd(nt, SignedSums(n_opts));
+    const int E = pay_exponent(S0);
+    std::vector<ExactSums> pa(nt, ExactSums(n_opts, E)), pg(nt, ExactSums(n_opts, E));
+    std::vector<SignedSums> pd(nt, SignedSums(n_opts, E));
 #pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
     for (int64_t k = (int64_t)path_lo; k < (int64_t)path_hi; ++k) {
 #ifdef _OPENMP
@@ -666,7 +689,7 @@ int oracle_price_paths_cv(const double *params7, double S0, uint32_t n_opts, con
         size_t last = 0;
         for (size_t j = 0; j < pr.T.size(); ++j)
             if (mat_paths[j] > (uint64_t)k) last = j;
-        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k));
+        OracleRNG rng(block_words, static_cast<uint32_t>(seed + (uint64_t)k), stream);
         run_path(pr, rng, false, [&](size_t j, double asian, double euro, double geo) {
             for (uint32_t o : pr.opts[j]) {
                 if ((uint64_t)k >= n_paths[o]) continue;
@@ -694,8 +717,8 @@ int oracle_price_paths_cv(const double *params7, double S0, uint32_t n_opts, con
         auto moments = [&](const uint64_t *d, bool biased, long double &mean, long double &var) {
             __int128 s1 = (__int128)ExactSums::value(d);
             if (biased) s1 -= (__int128)cnt << 63;
-            mean = cnt ? ((long double)s1 / 0x1p40L) / n : 0.L;
-            const long double m2 = cnt ? ((long double)ExactSums::value(d + 3) / 0x1p24L) / n : 0.L;
+            mean = cnt ? std::ldexp((long double)s1, E - 47) / n : 0.L;
+            const long double m2 = cnt ? std::ldexp((long double)ExactSums::value(d + 3), 2 * E - 43) / n : 0.L;
             var = cnt > 1 ? (m2 - mean * mean) * n / (n - 1) : 0.L;
             if (var < 0) var = 0;
         };

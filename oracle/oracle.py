@@ -71,10 +71,11 @@ def shishua_words(seed4, n_words: int) -> np.ndarray:
     return out
 
 
-def rng_draws(seed: int, block_words: int, kinds) -> np.ndarray:
+def rng_draws(seed: int, block_words: int, kinds, stream: int = 0) -> np.ndarray:
     k = np.ascontiguousarray(kinds, dtype=np.uint8)
     out = np.zeros(len(k))
-    lib().oracle_rng_draws(C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(block_words), _p(k), C.c_uint64(len(k)), _p(out))
+    lib().oracle_rng_draws(C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(stream & 0xFFFFFFFF), C.c_uint32(block_words),
+                           _p(k), C.c_uint64(len(k)), _p(out))
     return out
 
 
@@ -107,7 +108,8 @@ def _opts(strike, T, kind, n_paths, n_default):
 
 
 def price_paths(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
-                steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=None, threads=None):
+                steps_per_year=252.0, seed=42, stream=0, block_words=16, path_lo=0, path_hi=None, threads=None,
+                fast=False):
     """Per-path stream partition (the GPU's).  Returns (price, stderr, limbs[n,6] uint64)."""
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
     p = np.ascontiguousarray(params7, dtype=np.float64)
@@ -117,17 +119,19 @@ def price_paths(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, 
     sums = np.zeros(6 * n, dtype=np.uint64)
     hi = int(n_paths.max()) if path_hi is None else int(path_hi)
     th = threads or os.cpu_count() or 1
-    rc = lib().oracle_price_paths(_p(p), C.c_double(S0), C.c_uint32(n), _p(strike), _p(T), _p(kind), _p(n_paths),
-                                  C.c_uint32(step_mode), C.c_uint32(steps), C.c_double(steps_per_year),
-                                  C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(block_words), C.c_uint64(path_lo),
-                                  C.c_uint64(hi), C.c_int(th), _p(price), _p(se), _p(sums))
+    rc = lib(fast).oracle_price_paths(_p(p), C.c_double(S0), C.c_uint32(n), _p(strike), _p(T), _p(kind),
+                                      _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps),
+                                      C.c_double(steps_per_year), C.c_uint32(seed & 0xFFFFFFFF),
+                                      C.c_uint32(stream & 0xFFFFFFFF), C.c_uint32(block_words),
+                                      C.c_uint64(path_lo), C.c_uint64(hi), C.c_int(th), _p(price), _p(se),
+                                      _p(sums))
     if rc != 0:
         raise ValueError(f"oracle_price_paths failed: {rc}")
     return price, se, sums.reshape(n, 6)
 
 
 def branch_counts(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
-                  steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=None, threads=None):
+                  steps_per_year=252.0, seed=42, stream=0, block_words=16, path_lo=0, path_hi=None, threads=None):
     """(quadratic-branch QE steps, all QE steps) of the per-path partition."""
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
     p = np.ascontiguousarray(params7, dtype=np.float64)
@@ -136,8 +140,9 @@ def branch_counts(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536
     th = threads or os.cpu_count() or 1
     rc = lib().oracle_branch_counts(_p(p), C.c_double(S0), C.c_uint32(len(strike)), _p(strike), _p(T), _p(kind),
                                     _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps), C.c_double(steps_per_year),
-                                    C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(block_words), C.c_uint64(path_lo),
-                                    C.c_uint64(hi), C.c_int(th), _p(counts))
+                                    C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(stream & 0xFFFFFFFF),
+                                    C.c_uint32(block_words), C.c_uint64(path_lo), C.c_uint64(hi), C.c_int(th),
+                                    _p(counts))
     if rc != 0:
         raise ValueError(f"oracle_branch_counts failed: {rc}")
     return int(counts[0]), int(counts[1])
@@ -156,7 +161,7 @@ def geo_calls(params7, S0, strike, T, kind, *, step_mode=0, steps=252, steps_per
 
 
 def price_paths_cv(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
-                   steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=None, threads=None):
+                   steps_per_year=252.0, seed=42, stream=0, block_words=16, path_lo=0, path_hi=None, threads=None):
     """price_paths with the geometric control variate on the Asian options: (price, stderr)."""
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
     p = np.ascontiguousarray(params7, dtype=np.float64)
@@ -167,15 +172,15 @@ def price_paths_cv(params7, S0, strike, T, kind, n_paths=None, *, n_default=6553
     rc = lib().oracle_price_paths_cv(_p(p), C.c_double(S0), C.c_uint32(n), _p(strike), _p(T), _p(kind),
                                      _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps),
                                      C.c_double(steps_per_year), C.c_uint32(seed & 0xFFFFFFFF),
-                                     C.c_uint32(block_words), C.c_uint64(path_lo), C.c_uint64(hi), C.c_int(th),
-                                     _p(price), _p(se))
+                                     C.c_uint32(stream & 0xFFFFFFFF), C.c_uint32(block_words), C.c_uint64(path_lo),
+                                     C.c_uint64(hi), C.c_int(th), _p(price), _p(se))
     if rc != 0:
         raise ValueError(f"oracle_price_paths_cv failed: {rc}")
     return price, se
 
 
 def path_finals(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, step_mode=0, steps=252,
-                steps_per_year=252.0, seed=42, block_words=16, path_lo=0, path_hi=64):
+                steps_per_year=252.0, seed=42, stream=0, block_words=16, path_lo=0, path_hi=64):
     strike, T, kind, n_paths = _opts(strike, T, kind, n_paths, n_default)
     p = np.ascontiguousarray(params7, dtype=np.float64)
     m = len(np.unique(T))
@@ -185,8 +190,9 @@ def path_finals(params7, S0, strike, T, kind, n_paths=None, *, n_default=65536, 
     nm = C.c_uint32()
     rc = lib().oracle_path_finals(_p(p), C.c_double(S0), C.c_uint32(len(strike)), _p(strike), _p(T), _p(kind),
                                   _p(n_paths), C.c_uint32(step_mode), C.c_uint32(steps), C.c_double(steps_per_year),
-                                  C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(block_words), C.c_uint64(path_lo),
-                                  C.c_uint64(path_hi), _p(a), _p(e), C.byref(nm))
+                                  C.c_uint32(seed & 0xFFFFFFFF), C.c_uint32(stream & 0xFFFFFFFF),
+                                  C.c_uint32(block_words), C.c_uint64(path_lo), C.c_uint64(path_hi), _p(a), _p(e),
+                                  C.byref(nm))
     if rc != 0:
         raise ValueError(f"oracle_path_finals failed: {rc}")
     return a.reshape(n, m), e.reshape(n, m)

@@ -189,7 +189,7 @@ def test_host_finaliser_from_oracle_limbs(lib, oracle):
     price, se, limbs = oracle.price_paths(p.as_array(), 100.0, K, 1.0, [0, 1, 0], n_default=4000, steps=60)
     opts = E.Options(K, 1.0, np.array([0, 1, 0]))
     cfg = E.Config(n_paths=4000, steps=60)
-    fp, fse = E.finalize_limbs(p, opts, cfg, limbs)
+    fp, fse = E.finalize_limbs(p, 100.0, opts, cfg, limbs)
     np.testing.assert_allclose(fp, price, rtol=1e-14)
     np.testing.assert_allclose(fse, se, rtol=1e-9)
 

@@ -24,7 +24,7 @@ def oracle_cv(oracle, req, cfg):
     o = req.options
     return oracle.price_paths_cv(req.params.as_array(), req.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths,
                                  n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
-                                 steps_per_year=cfg.steps_per_year, seed=req.seed)
+                                 steps_per_year=cfg.steps_per_year, seed=req.seed, stream=req.stream)
 
 
 @pytest.mark.parametrize("maker", [W.single_chain, W.feller_violating, W.plain_asian])

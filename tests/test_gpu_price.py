@@ -25,7 +25,7 @@ def oracle_price(oracle, req, cfg, **kw):
     o = req.options
     return oracle.price_paths(req.params.as_array(), req.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths,
                               n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
-                              steps_per_year=cfg.steps_per_year, seed=req.seed, **kw)
+                              steps_per_year=cfg.steps_per_year, seed=req.seed, stream=req.stream, **kw)
 
 
 def assert_fp64_close(got, want, S0):
@@ -172,7 +172,7 @@ def test_shards_merge_bit_identical(engine):
     a = engine.partial(req.params, req.S0, req.options, cfg, 0, 2500)
     b = engine.partial(req.params, req.S0, req.options, cfg, 2500, 6000)
     assert np.array_equal(full, a + b)
-    p_merge, se_merge = E.finalize_limbs(req.params, req.options, cfg, a + b)
+    p_merge, se_merge = E.finalize_limbs(req.params, req.S0, req.options, cfg, a + b)
     p, se = engine.price(req.params, req.S0, req.options, cfg)
     assert np.array_equal(p, p_merge) and np.array_equal(se, se_merge)
 
@@ -215,14 +215,6 @@ def test_single_path_and_tiny_maturity(engine, oracle):
     assert p[2] == 0.0
 
 
-def test_numeric_range_error(engine):
-    params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5)
-    opts = E.Options(np.array([0.0]), 1.0, 1)
-    with pytest.raises(HexoError) as ei:
-        engine.price(params, 1e8, opts, E.Config(n_paths=64, steps=10))
-    assert ei.value.status == 6
-
-
 def test_invalid_request_errors(engine):
     params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5)
     with pytest.raises(HexoError) as ei:
@@ -263,7 +255,7 @@ def test_parameter_edges_fp64_vs_oracle_and_fp32(engine, oracle, k):
 
 
 def test_extreme_spot_levels(engine, oracle):
-    for S0 in (1e-3, 1e4):
+    for S0 in (2.0 ** -60, 1e-3, 1e4, 1e8, 2.0 ** 59):
         params = E.Params(0.04, 0.04, -0.7, 1.5, 0.5, 0.02)
         K = S0 * np.array([0.8, 1.0, 1.2])
         req = E.Request(params, S0, E.Options(K, 1.0, E.ASIAN), seed=3)

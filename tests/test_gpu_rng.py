@@ -32,6 +32,29 @@ def test_shishua_seed_wraps_mod_2_32(engine, oracle):
         assert np.array_equal(got[k], want), k
 
 
+@pytest.mark.parametrize("stream", [1, 63, 0xFFFFFFFF])
+def test_shishua_words_with_stream_word(engine, oracle, stream):
+    # seed word 1 (the request's stream number) enters the state as SHISHUA's
+    # init places it; stream 0 is the reference class's {seed, 0, 0, 0}
+    seed = 3035318956
+    got = engine.rng_words(seed, 64, 48, stream=stream)
+    for k in (0, 5, 63):
+        want = oracle.shishua_words([(seed + k) & 0xFFFFFFFF, stream, 0, 0], 48)
+        assert np.array_equal(got[k], want), (k, stream)
+    base = engine.rng_words(seed, 64, 48)
+    assert not any(np.array_equal(got[k], base[k]) for k in range(64))
+
+
+def test_two_buffer_draws_with_stream_word(engine, oracle):
+    rng = np.random.default_rng(9)
+    kinds = (rng.random(900) < 0.2).astype(np.uint8)
+    seed, n_streams, stream = 77, 64, 12345
+    got = engine.rng_draws(seed, n_streams, kinds, stream=stream)
+    for k in range(0, n_streams, 9):
+        want = oracle.rng_draws(seed + k, 16, kinds, stream=stream)
+        assert np.array_equal(got[k].view(np.uint64), want.view(np.uint64)), k
+
+
 @pytest.mark.parametrize("p_uniform", [0.0, 0.02, 0.3, 0.5, 1.0])
 def test_two_buffer_draws(engine, oracle, p_uniform):
     rng = np.random.default_rng(int(p_uniform * 1000) + 1)

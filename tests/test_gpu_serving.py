@@ -100,7 +100,8 @@ def test_requests_from_paramsdb(engine, tmp_path):
         for k, rq in enumerate(reqs):
             db.insertupdate(rq.params, f"U{k}")
         # the table holds the five Heston parameters; the rate comes with the request
-        from_db = [db.request(f"U{k}", rq.S0, rq.options, seed=rq.seed, r=rq.params.r) for k, rq in enumerate(reqs)]
+        from_db = [db.request(f"U{k}", rq.S0, rq.options, seed=rq.seed, r=rq.params.r,
+                              stream=rq.stream) for k, rq in enumerate(reqs)]
     with engine.server(cfg) as srv:
         got = [srv.wait(srv.submit(rq)) for rq in from_db]
     for rq, (p, s) in zip(reqs, got):

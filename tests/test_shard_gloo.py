@@ -33,7 +33,7 @@ def _request():
     keep = slice(0, 12)   # a dozen options keep the oracle quick
     o = rq.options
     rq = E.Request(rq.params, rq.S0, E.Options(o.strike[keep], o.T[keep], o.payoff[keep], o.n_paths[keep]),
-                   seed=rq.seed)
+                   seed=rq.seed, stream=7)
     return rq, cfg
 
 
@@ -42,7 +42,8 @@ def _oracle_partial(rq, cfg, lo, hi):
     o = rq.options
     _, _, limbs = O.price_paths(rq.params.as_array(), rq.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths,
                                 n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
-                                steps_per_year=cfg.steps_per_year, seed=rq.seed, path_lo=lo, path_hi=hi)
+                                steps_per_year=cfg.steps_per_year, seed=rq.seed, stream=rq.stream, path_lo=lo,
+                                path_hi=hi)
     return limbs
 
 
@@ -73,7 +74,7 @@ def test_gloo_shards_merge_bit_identical(tmp_path, oracle, world):
                        start_method="spawn")
     rq, cfg = _request()
     full = _oracle_partial(rq, cfg, 0, S.max_paths(rq, cfg))
-    want = np.stack(E.finalize_limbs(rq.params, rq.options, cfg, full))
+    want = np.stack(E.finalize_limbs(rq.params, rq.S0, rq.options, cfg, full))
     for r in range(world):
         got = np.load(tmp_path / f"r{r}.npy")
         assert np.array_equal(got, want), r
@@ -81,5 +82,5 @@ def test_gloo_shards_merge_bit_identical(tmp_path, oracle, world):
     p_or, se_or, _ = oracle.price_paths(rq.params.as_array(), rq.S0, rq.options.strike, rq.options.T,
                                         rq.options.payoff.astype(np.uint8), rq.options.n_paths,
                                         n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
-                                        steps_per_year=cfg.steps_per_year, seed=rq.seed)
+                                        steps_per_year=cfg.steps_per_year, seed=rq.seed, stream=rq.stream)
     np.testing.assert_allclose(want[0], p_or, rtol=1e-14, atol=1e-14)

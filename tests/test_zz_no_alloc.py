@@ -60,3 +60,17 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     one = E.Options(np.array([100.0]), 1.0, 0)
     st, _, _ = noalloc(params, 100.0, one, E.Config(n_paths=(1 << 20) + 1, steps=10))
     assert st == 10
+
+
+def test_noalloc_after_calls_with_smaller_launch_shapes(engine):
+    # the allocating entry points launch the same path kernels with other
+    # launch shapes (here 128-thread CTAs, whose shared memory is smaller);
+    # the kernels' shared-memory limit is the same for every caller, so the
+    # no-allocation call after them still launches its 256-thread CTAs
+    params, S0, opts, cfg = cases()[1]
+    for prec in (E.FP64, E.FP32):
+        small = E.Config(**{**cfg.__dict__, "precision": prec, "block": 128})
+        want_p, want_se = engine.price(params, S0, opts, small)
+        st, p, se = noalloc(params, S0, opts, E.Config(**{**cfg.__dict__, "precision": prec}))
+        assert st == 0, L.STATUS_NAMES.get(st, st)
+        assert np.array_equal(p, want_p) and np.array_equal(se, want_se)
