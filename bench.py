@@ -12,18 +12,21 @@ CUDA graph.  Synthetic data (the reference prices live Tradier chains).
              between timed launches
   e2e        the same metric through hexo_price_batch with host buffers
              (planning, upload, run and result download inside the timing)
-  fp64       the plain FP64 form, one request per launch, on a sample of the
-             sets, and the FP32 form's error against it
+  fp64_plain the plain FP64 form, one request per launch, on every set at
+             full paths: device-timed and end to end, the FP32 form's
+             speed-up over it and its error against it (the last key)
   roofline   the path kernel's algorithmic operations per second on the pipe
              that binds (FP32 FMA, MUFU or integer ALU, each against this
              GPU's lane rate measured in the run), with the branch mix p_Q
              the kernel counted
-  serving    Poisson request streams through the continuous-batching server
-             (FP32), p50/p99 submit-to-completion latency, against the same
-             streams priced one request per plain FP64 launch
+  serving    Poisson request streams (50-2000 req/s, at least 1,000
+             requests each) through the continuous-batching server (FP32),
+             p50/p99 submit-to-completion latency, against the first requests
+             of each stream priced one per plain FP64 launch
   cpu_baseline / --impl reference
              the oracle port of the reference's CPU path (OpenMP over all
-             host cores) on a bounded sample of the same workload
+             host cores) on the same bounded sample in both arms: all 64 sets
+             at 1/256 of their paths, its work counted by the oracle
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
   python bench.py --precision-sweep | --swift | --configs | --autotune [--path-scale S]   (reports, not the benchmark)
@@ -75,10 +78,12 @@ def alg_ops_per_path_step(p: float) -> dict:
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
 # Nsight Compute capture of this workload at 1/16 of its paths (129.0 MB +
-# 87.3 MB; profiles/paths_kernel_fp32_uneven64_x0.0625_launches.md).  The
-# traffic is the CTA-private sum slots a launch touches plus the descriptors;
-# it does not grow with the path count, so it is reported unscaled.
+# 87.3 MB).  The traffic is the CTA-private sum slots a launch touches plus
+# the descriptors; it does not grow with the path count, so it is reported
+# unscaled.
 PATHS_KERNEL_DRAM_BYTES = 129.0e6 + 87.3e6
+PATHS_KERNEL_DRAM_NOTE = ("DRAM bytes per launch from ncu at 1/16 of the paths; sum slots and descriptors, "
+                          "independent of the path count")
 
 
 def dist_env():
@@ -145,50 +150,63 @@ def plan_stats(reqs, cfg):
 
 # ------------------------------------------------------------ CPU baseline
 
-def cpu_sample(rank: int):
-    """A bounded sample of the workload for the CPU: the first two sets with
-    every path count divided by 4 (same maturities, strikes and schedule;
-    about 2.3e9 nominal path-steps, 10-30 s on a few dozen cores)."""
+CPU_PATH_SCALE = 1 / 256
+
+
+def workload_config():
+    """The workload both arms name: the same dict in the engine line and in
+    the reference line."""
     from hestonexotics_gb300 import workloads as W
-    reqs, cfg = W.uneven_batch(seed=2 + rank, path_scale=1 / 4)
-    return reqs[:2], cfg
+    from oracle import oracle as O
+    reqs, _ = W.uneven_batch(seed=2)
+    return {"workload": WORKLOAD, "sets": len(reqs), "seed": 2,
+            "options": int(sum(len(r.options) for r in reqs)),
+            "nominal_path_steps": int(sum(O.nominal_path_steps(r.options.T, r.options.n_paths) for r in reqs)),
+            "paths": "2^14-2^22 per distinct maturity, log-uniform", "step_mode": "grid 252/y",
+            "payoffs": "Asian:European 3:1"}
 
 
-def run_cpu_baseline(rank: int, steps: int = 1):
+def cpu_sample(rank: int):
+    """A bounded sample of the workload for the CPU: all 64 sets, every path
+    count scaled by 1/256 (same parameter sets, maturities, strikes, step
+    schedules and branch mix; 1.16e9 nominal path-steps, a few seconds on a
+    few dozen cores).  Its work is counted by the oracle's own walk of the
+    time grid, so the CPU legs load no engine code."""
+    from hestonexotics_gb300 import workloads as W
+    from oracle import oracle as O
+    reqs, cfg = W.uneven_batch(seed=2 + rank, path_scale=CPU_PATH_SCALE)
+    nominal = sum(O.nominal_path_steps(r.options.T, r.options.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
+                                       steps_per_year=cfg.steps_per_year) for r in reqs)
+    return reqs, cfg, nominal
+
+
+def cpu_sample_step(O, reqs, cfg, threads):
+    t0 = time.perf_counter()
+    for rq in reqs:
+        _oracle_price_fast(O, rq, cfg, threads)
+    return time.perf_counter() - t0
+
+
+def run_cpu_baseline(rank: int, steps: int = 3):
     from oracle import oracle as O
     O.build()
-    reqs, cfg = cpu_sample(rank)
+    reqs, cfg, nominal = cpu_sample(rank)
     threads = os.cpu_count() or 1
-    nominal = plan_stats(reqs, cfg).nominal_path_steps
-    times = []
-    for _ in range(max(1, steps)):
-        t0 = time.perf_counter()
-        for rq in reqs:
-            _oracle_price_fast(O, rq, cfg, threads)
-        times.append(time.perf_counter() - t0)
+    cpu_sample_step(O, reqs[:4], cfg, threads)      # warm-up: page in, spin up the thread pool
+    times = [cpu_sample_step(O, reqs, cfg, threads) for _ in range(max(1, steps))]
     t = statistics.median(times)
     return {"value": nominal / t, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first 2 of the 64 sets with path counts / 4 ({nominal:.3e} nominal path-steps), "
-                      f"oracle port of the reference loop (-O3 -ffast-math, OpenMP {threads} threads), "
-                      f"median of {len(times)}", "seconds": t}
+            "sample": f"all 64 sets with every path count x{CPU_PATH_SCALE:g} ({nominal:.3e} nominal path-steps, "
+                      f"counted by the oracle), oracle port of the reference loop (-O3 -ffast-math, OpenMP "
+                      f"{threads} threads), median of {len(times)}", "seconds": t, "nominal_path_steps": nominal}
 
 
 def _oracle_price_fast(O, rq, cfg, threads):
-    import ctypes as C
     o = rq.options
-    strike, T, kind, n_paths = O._opts(o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths, cfg.n_paths)
-    p = np.ascontiguousarray(rq.params.as_array())
-    n = len(strike)
-    price, se = np.zeros(n), np.zeros(n)
-    limbs = np.zeros(6 * n, dtype=np.uint64)
-    rc = O.lib(fast=True).oracle_price_paths(
-        O._p(p), C.c_double(rq.S0), C.c_uint32(n), O._p(strike), O._p(T), O._p(kind), O._p(n_paths),
-        C.c_uint32(cfg.step_mode), C.c_uint32(cfg.steps), C.c_double(cfg.steps_per_year),
-        C.c_uint32(rq.seed & 0xFFFFFFFF), C.c_uint32(16), C.c_uint64(0), C.c_uint64(int(n_paths.max())),
-        C.c_int(threads), O._p(price), O._p(se), O._p(limbs))
-    if rc != 0:
-        raise RuntimeError("oracle failed")
-    return price, se, limbs
+    return O.price_paths(rq.params.as_array(), rq.S0, o.strike, o.T, o.payoff.astype(np.uint8), o.n_paths,
+                         n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
+                         steps_per_year=cfg.steps_per_year, seed=rq.seed, stream=rq.stream, threads=threads,
+                         fast=True)
 
 
 # -------------------------------------------------------------- serving
@@ -197,18 +215,19 @@ def _pct(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if xs else None
 
 
-def run_serving(eng, rates, duration_s, fp64_rates):
-    """Open-loop Poisson request streams (workloads.request_stream) against
-    the continuous-batching server (FP32 form), and the same streams priced
-    one request per launch in the plain FP64 form, first come first served.
-    Latency is submit (arrival) to completion."""
+def run_serving(eng, rates, min_requests, min_seconds, fp64_requests):
+    """Open-loop Poisson request streams (workloads.request_stream, seed 3)
+    against the continuous-batching server (FP32 form), each rate run for at
+    least min_seconds and min_requests arrivals, and the first fp64_requests
+    arrivals of the same stream priced one request per plain FP64 launch,
+    first come first served.  Latency is submit (arrival) to completion."""
     from hestonexotics_gb300 import FP64
     from hestonexotics_gb300 import workloads as W
-    from hestonexotics_gb300._lib import HEXO_OK
     out = []
     for rate in rates:
-        arrivals, cfg = W.request_stream(rate, duration_s, seed=3)
-        row = {"rate_per_s": rate, "requests": len(arrivals), "seconds": duration_s}
+        duration = max(min_seconds, min_requests / rate)
+        arrivals, cfg = W.request_stream(rate, duration, seed=3)
+        row = {"rate": rate, "requests": len(arrivals), "seconds": round(duration, 2)}
         srv = eng.server(cfg, max_batch_requests=64, max_inflight=3)
         prepared = [srv.prepare(a.request) for a in arrivals]
         tickets = []
@@ -228,24 +247,67 @@ def run_serving(eng, rates, duration_s, fp64_rates):
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        row["server_fp32"] = {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
-                              "completed": ok, "launches": st["batches"], "queued_max": st["queued_max"],
-                              "mem_peak_bytes": st["mem_peak"],
-                              "path_steps_per_s": st["nominal_path_steps"] / wall}
-        if rate in fp64_rates:
+        row["fp32"] = {"p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
+                       "mean_ms": round(st["mean_ms"], 2), "completed": ok, "launches": st["batches"],
+                       "queued_max": st["queued_max"], "mem_peak_mb": round(st["mem_peak"] / 2 ** 20, 1),
+                       "path_steps_per_s": st["nominal_path_steps"] / wall}
+        if fp64_requests:
             cfg64 = type(cfg)(**{**cfg.__dict__, "precision": FP64})
             lat = []
+            sub = arrivals[:fp64_requests]
             t0 = time.perf_counter()
-            for a in arrivals:
+            for a in sub:
                 d = t0 + a.t - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
                 eng.price_batch([a.request], cfg64)
                 lat.append((time.perf_counter() - (t0 + a.t)) * 1e3)
-            row["plain_fp64_one_per_launch"] = {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
-                                                "mean_ms": float(np.mean(lat)), "completed": len(lat)}
+            row["fp64_one_per_launch"] = {"p50_ms": round(_pct(lat, 50), 2), "p99_ms": round(_pct(lat, 99), 2),
+                                          "completed": len(lat)}
         out.append(row)
     return out
+
+
+# ------------------------------------------------------- plain FP64 form
+
+def run_fp64_plain(eng, reqs, cfg64, fp32_outputs, flush, stream):
+    """The plain FP64 form on every set of the batch, one request per launch:
+    device time of each request's graph launch with CUDA events on the
+    engine's stream (L2 flushed before each), and end to end per request
+    through the public calls with host buffers (hexo_batch_prepare: planning
+    and upload; hexo_batch_launch; hexo_batch_collect: the download).  The
+    FP32 prices of the timed batch are checked against these FP64 prices on
+    the same streams."""
+    import torch
+    dev_ms, e2e_s, nominal = 0.0, 0.0, 0
+    rel, n_big, in_se, n_opts = 0.0, 0, 0, 0
+    for rq, (p32, se32) in zip(reqs, fp32_outputs):
+        t0 = time.perf_counter()
+        b = eng.prepare_batch([rq], cfg64)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        t1 = time.perf_counter()
+        b.launch()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        (p64, _), = b.collect()
+        t2 = time.perf_counter()
+        nominal += b.info()["nominal_path_steps"]
+        b.close()
+        e2e_s += (t1 - t0) + (t2 - t1)
+        dev_ms += e0.elapsed_time(e1)
+        big = p64 > 1e-3 * rq.S0
+        if big.any():
+            rel = max(rel, float(np.max(np.abs(p32[big] - p64[big]) / p64[big])))
+        n_big += int(big.sum())
+        in_se += int(np.sum(np.abs(p32 - p64) <= np.maximum(se32, 1e-9 * rq.S0)))
+        n_opts += len(p64)
+    return {"value": nominal / (dev_ms * 1e-3), "e2e": nominal / e2e_s, "sets": len(reqs),
+            "nominal_path_steps": nominal, "device_s": dev_ms * 1e-3, "e2e_s": e2e_s,
+            "fp32_vs_fp64_max_rel_err": rel, "prices_checked": n_big, "fp32_within_1se_frac": in_se / max(1, n_opts)}
 
 
 # ------------------------------------------------------ precision sweep
@@ -500,45 +562,16 @@ def run_engine(args, rank, world, local):
             e2e_s.append(time.perf_counter() - t0)
         e2e_value = nominal / statistics.median(e2e_s)
 
-        # plain FP64 form, one request per launch, on a sample of sets
-        n_fp64 = min(args.fp64_sets, len(reqs))
-        cfg64 = W.uneven_batch(seed=2, precision=FP64)[1]
-        nom64 = plan_stats(reqs[:n_fp64], cfg64).nominal_path_steps
-        t0 = time.perf_counter()
-        # one request per launch, each on its own seed, as the batch prices it
-        p64 = [eng.price_batch([rq], cfg64)[0] for rq in reqs[:n_fp64]]
-        fp64_s = time.perf_counter() - t0
-        fp64_value = nom64 / fp64_s
-        rel, in_se, n_big = 0.0, 0, 0
-        n_opts = 0
-        for (pa, sa), (pb, _) in zip(fp32_outputs[:n_fp64], p64):
-            big = pb > 1e-3 * 100.0
-            if big.any():
-                rel = max(rel, float(np.max(np.abs(pa[big] - pb[big]) / pb[big])))
-            n_big += int(big.sum())
-            in_se += int(np.sum(np.abs(pa - pb) <= np.maximum(sa, 1e-9)))
-            n_opts += len(pa)
-
-        # every set of the batch at 1/16 of its paths: FP32 against FP64 on the same streams
-        reqs16, cfg16 = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale / 16)
-        cfg16_64 = W.uneven_batch(seed=2, precision=FP64, path_scale=args.path_scale / 16)[1]
-        o32 = eng.price_batch(reqs16, cfg16)
-        o64 = eng.price_batch(reqs16, cfg16_64)
-        all_rel, all_in_se, all_n, all_big = 0.0, 0, 0, 0
-        for rq, (pa, sa), (pb, _) in zip(reqs16, o32, o64):
-            big = pb > 1e-3 * rq.S0
-            if big.any():
-                all_rel = max(all_rel, float(np.max(np.abs(pa[big] - pb[big]) / pb[big])))
-            all_big += int(big.sum())
-            all_in_se += int(np.sum(np.abs(pa - pb) <= np.maximum(sa, 1e-9)))
-            all_n += len(pa)
+        # the plain FP64 form on every set, one request per launch
+        cfg64 = type(cfg)(**{**cfg.__dict__, "precision": FP64})
+        fp64 = run_fp64_plain(eng, reqs, cfg64, fp32_outputs, flush, stream)
 
         peaks = eng.pipe_peaks()
         kms = statistics.mean(kernel_ms)
         # per pipe: the path-steps/s its measured peak allows; the smallest binds
         ops = alg_ops_per_path_step(p_quad)
         rate = nominal / (kms * 1e-3)
-        pipes = {k: {"ops_per_path_step": ops[k], "peak_lane_ops_per_s": peaks[k],
+        pipes = {k: {"ops_per_path_step": round(ops[k], 2), "peak_lane_ops_per_s": peaks[k],
                      "bound_path_steps_per_s": peaks[k] / ops[k], "frac": rate / (peaks[k] / ops[k])}
                  for k in ops}
         bind = min(pipes, key=lambda k: pipes[k]["bound_path_steps_per_s"])
@@ -547,44 +580,43 @@ def run_engine(args, rank, world, local):
         serving = None
         if args.serve_rates:
             rates = [float(x) for x in args.serve_rates.split(",") if x]
-            fp64_rates = [float(x) for x in args.serve_fp64_rates.split(",") if x]
-            serving = run_serving(eng, rates, args.serve_seconds, fp64_rates)
-        cpu = run_cpu_baseline(rank)
+            serving = run_serving(eng, rates, args.serve_min_requests, args.serve_seconds, args.serve_fp64_requests)
+        cpu = run_cpu_baseline(rank, steps=3)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f32 AS241, exact integer sums, f64 finalise",
             "data": "synthetic (seeded uneven 64-set batch; the reference prices live option chains)",
-            "config": {"workload": WORKLOAD if args.path_scale == 1.0 else f"{WORKLOAD}_paths_x{args.path_scale:g}",
-                       "sets": len(reqs), "options": info["n_options"],
-                       "paths": info["n_paths"], "nominal_path_steps": nominal,
-                       "executed_path_steps": info["executed_path_steps"], "tiles": info["n_tiles"],
-                       "block": info["block"], "paths_per_thread": info["paths_per_thread"],
+            "config": workload_config() if args.path_scale == 1.0 else
+            {**workload_config(), "workload": f"{WORKLOAD}_paths_x{args.path_scale:g}"},
+            "launch": {"form": "FP32, one persistent launch of the whole batch through a captured CUDA graph",
+                       "paths": info["n_paths"], "executed_path_steps": info["executed_path_steps"],
+                       "tiles": info["n_tiles"], "block": info["block"], "paths_per_thread": info["paths_per_thread"],
                        "unroll": info["unroll"], "grid": info["grid"], "l2": "flushed between timed launches",
-                       "step_mode": "grid 252/y", "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
-                    "d2h_bytes_per_step": info["d2h_bytes"]},
-            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
-                           "what": "graph launch of the whole batch"},
-            "fp64_plain": {"value": fp64_value, "unit": UNIT, "sets": n_fp64, "nominal_path_steps": nom64,
-                           "fp32_speedup": value / fp64_value,
-                           "fp32_vs_fp64_max_rel_err": rel, "options_checked": n_big,
-                           "fp32_within_1se_frac": in_se / max(1, n_opts),
-                           "all_64_sets_at_1_16_paths": {"fp32_vs_fp64_max_rel_err": all_rel,
-                                                         "options_checked": all_big,
-                                                         "fp32_within_1se_frac": all_in_se / max(1, all_n)}},
+                    "d2h_bytes_per_step": info["d2h_bytes"],
+                    "what": "hexo_price_batch with host buffers: planning, upload, run, download"},
             "roofline": {"bound": f"compute: {bind} pipe (no tensor-core or HBM bound on this path)",
                          "achieved": achieved, "peak": peak, "unit": f"Gop/s ({bind} lane ops)",
                          "frac": achieved / peak, "traffic": PATHS_KERNEL_DRAM_BYTES,
-                         "traffic_note": "DRAM bytes per launch from ncu at 1/16 of the paths; sum slots and "
-                                         "descriptors, independent of the path count",
+                         "traffic_note": PATHS_KERNEL_DRAM_NOTE,
                          "peak_source": "lane rates measured in this run by hexo_debug_pipe_peaks (of measured)",
                          "p_quadratic": p_quad, "as241_central_share": AS241_CENTRAL,
-                         "pipes": pipes, "kernel_ms": kms, "pipe_peaks_lane_ops_per_s": peaks},
+                         "pipes": pipes, "kernel_ms": kms},
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                           "what": "graph launch of the whole batch"},
             "serving": serving,
-            "cpu_baseline": cpu,
+            "cpu_baseline": {k: v for k, v in cpu.items() if k != "nominal_path_steps"},
             "clocks": clk,
-            "gpu_launches": (args.steps) * 2,
+            "gpu_launches": args.steps * 2,
+            "fp64_plain": {"value": fp64["value"], "e2e": fp64["e2e"], "unit": UNIT, "sets": fp64["sets"],
+                           "fp32_speedup": value / fp64["value"], "fp32_speedup_e2e": e2e_value / fp64["e2e"],
+                           "fp32_vs_fp64_max_rel_err": fp64["fp32_vs_fp64_max_rel_err"],
+                           "prices_checked": fp64["prices_checked"],
+                           "fp32_within_1se_frac": fp64["fp32_within_1se_frac"],
+                           "what": "one request per launch, all sets, full paths; value device-timed, e2e "
+                                   "through hexo_batch_prepare/launch/collect"},
         }
     eng.close()
     if world > 1:
@@ -594,20 +626,28 @@ def run_engine(args, rank, world, local):
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle port; the reference itself is a
+    C++ command-line program that cannot be installed as a package) on all
+    host cores, each step the bounded sample of the workload that
+    cpu_sample names; no engine code is loaded."""
     if rank != 0:
         return None
-    steps = []
-    res = None
-    for _ in range(max(1, args.steps)):
-        res = run_cpu_baseline(rank)
-        steps.append(res["seconds"])
-    value = res["value"]
+    from oracle import oracle as O
+    O.build()
+    reqs, cfg, nominal = cpu_sample(rank)
+    threads = os.cpu_count() or 1
+    for _ in range(max(0, args.warmup)):
+        cpu_sample_step(O, reqs, cfg, threads)
+    steps = [cpu_sample_step(O, reqs, cfg, threads) for _ in range(max(1, args.steps))]
+    value = nominal * len(steps) / sum(steps)
+    sample = (f"all 64 sets with every path count x{CPU_PATH_SCALE:g} ({nominal:.3e} nominal path-steps per step, "
+              f"counted by the oracle), oracle port of the reference loop (-O3 -ffast-math, OpenMP {threads} threads)")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(steps), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference CPU path)",
-            "data": "synthetic (seeded uneven 64-set batch, bounded sample)",
-            "config": {"workload": WORKLOAD, "sample": res["sample"]}, "impl": "reference",
-            "cpu_baseline": {"kind": res["kind"], "cores": res["cores"], "sample": res["sample"], "value": value},
+            "data": "synthetic (seeded uneven 64-set batch, bounded sample per step)",
+            "config": workload_config(), "impl": "reference",
+            "cpu_baseline": {"kind": "port", "cores": threads, "sample": sample, "value": value},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -617,10 +657,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--fp64-sets", type=int, default=2)
-    ap.add_argument("--serve-rates", default="50,200,500,2000", help="request rates of the serving leg ('' = skip)")
-    ap.add_argument("--serve-fp64-rates", default="50,200", help="rates also priced one request per FP64 launch")
-    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-rates", default="50,200,500,1000,2000",
+                    help="request rates of the serving leg ('' = skip)")
+    ap.add_argument("--serve-min-requests", type=int, default=1000,
+                    help="each rate runs until at least this many requests have arrived")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="and for at least this long")
+    ap.add_argument("--serve-fp64-requests", type=int, default=300,
+                    help="the first requests of each stream also priced one per plain FP64 launch (0 = skip)")
     ap.add_argument("--precision-sweep", action="store_true",
                     help="instead of the benchmark: FP32 vs FP64 errors on the single chain at 2^16..2^24 paths")
     ap.add_argument("--swift", action="store_true",

@@ -87,12 +87,12 @@ class hexo_tune_entry(C.Structure):
 
 class hexo_server_opts(C.Structure):
     _fields_ = [("cfg", hexo_mc_cfg), ("mem_cap_bytes", C.c_uint64), ("max_batch_requests", C.c_uint32),
-                ("max_inflight", C.c_uint32)]
+                ("max_inflight", C.c_uint32), ("launch_path_steps", C.c_uint64)]
 
 
 class hexo_server_stats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
-                ("failed", C.c_uint64), ("batches", C.c_uint64), ("queued_now", C.c_uint64),
+                ("failed", C.c_uint64), ("batches", C.c_uint64), ("chunks", C.c_uint64), ("queued_now", C.c_uint64),
                 ("queued_max", C.c_uint64), ("inflight_now", C.c_uint64), ("mem_in_use", C.c_uint64),
                 ("mem_peak", C.c_uint64), ("nominal_path_steps", C.c_uint64), ("busy_seconds", C.c_double),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double)]

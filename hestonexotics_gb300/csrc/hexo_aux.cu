@@ -25,48 +25,56 @@ cudaError_t paths_smem_limit(const void *fn, int dev) {
 }
 
 // Sums the CTA-private copies of the limbs (exact integer additions) and
-// finalises each option.
-__global__ void finalize_kernel(const unsigned long long *__restrict__ acc, uint32_t n_slots, uint64_t slot_stride,
-                                const uint64_t *__restrict__ n_paths, const double *__restrict__ disc,
-                                const int32_t *__restrict__ pay_exp, uint32_t n,
-                                double *__restrict__ price, double *__restrict__ se,
-                                unsigned long long *__restrict__ acc_sum, const double *__restrict__ cv_eg,
-                                const uint32_t *__restrict__ cv_partner) {
+// finalises each option.  With carried sums (the serving loop's requests
+// that run as several path blocks across launches), a slot's totals are
+// first added into its request's running sums in device memory, and only
+// the launch that carries the request's last block finalises, from those.
+__global__ void finalize_kernel(const FinalizeArgs f) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= f.n) return;
     auto total = [&](uint32_t o, uint64_t (&l)[kLimbs]) {
 #pragma unroll
         for (int x = 0; x < kLimbs; ++x) l[x] = 0;
-        for (uint32_t s = 0; s < n_slots; ++s)
+        for (uint32_t s = 0; s < f.n_slots; ++s)
 #pragma unroll
-            for (int x = 0; x < kLimbs; ++x) l[x] += acc[(size_t)s * slot_stride + (size_t)o * kLimbs + x];
+            for (int x = 0; x < kLimbs; ++x) l[x] += f.acc[(size_t)s * f.slot_stride + (size_t)o * kLimbs + x];
     };
     uint64_t l[kLimbs];
     total(i, l);
-    if (acc_sum != nullptr)
+    if (f.acc_sum != nullptr)
 #pragma unroll
-        for (int x = 0; x < kLimbs; ++x) acc_sum[(size_t)i * kLimbs + x] = l[x];
+        for (int x = 0; x < kLimbs; ++x) f.acc_sum[(size_t)i * kLimbs + x] = l[x];
+    const uint64_t cr = f.carry_row != nullptr ? f.carry_row[i] : ~0ull;
+    if (cr != ~0ull) {   // one launch at a time touches a request's running sums
+        unsigned long long *row = f.carry + (size_t)(cr >> 1) * kLimbs;
+#pragma unroll
+        for (int x = 0; x < kLimbs; ++x) {
+            row[x] += l[x];
+            l[x] = row[x];
+        }
+        if ((cr & 1ull) == 0ull) {   // more blocks to come
+            f.price[i] = __longlong_as_double(0x7ff8000000000000ll);
+            f.se[i] = __longlong_as_double(0x7ff8000000000000ll);
+            return;
+        }
+    }
     double p, s;
-    const uint32_t g = cv_partner != nullptr ? cv_partner[i] : ~0u;
+    const uint32_t g = f.cv_partner != nullptr ? f.cv_partner[i] : ~0u;
     if (g != ~0u) {   // an Asian option with the control variate: its geometric and difference sums
         uint64_t lg[kLimbs], ld[kLimbs];
         total(g, lg);
         total(g + 1u, ld);
-        finalize_cv(l, lg, ld, n_paths[i], disc[i], pay_exp[i], cv_eg[i], &p, &s);
+        finalize_cv(l, lg, ld, f.n_paths[i], f.disc[i], f.pay_exp[i], f.cv_eg[i], &p, &s);
     } else {
-        finalize_limbs6(l, n_paths[i], disc[i], pay_exp[i], &p, &s);
+        finalize_limbs6(l, f.n_paths[i], f.disc[i], f.pay_exp[i], &p, &s);
     }
-    price[i] = p;
-    se[i] = s;
+    f.price[i] = p;
+    f.se[i] = s;
 }
 
-cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
-                            const uint64_t *n_paths, const double *disc, const int32_t *pay_exp, uint32_t n,
-                            double *price, double *se, unsigned long long *acc_sum, cudaStream_t st,
-                            const double *cv_eg, const uint32_t *cv_partner) {
-    if (n == 0) return cudaSuccess;
-    finalize_kernel<<<(n + 255) / 256, 256, 0, st>>>(acc, n_slots, slot_stride, n_paths, disc, pay_exp, n, price, se,
-                                                      acc_sum, cv_eg, cv_partner);
+cudaError_t launch_finalize(const FinalizeArgs &f, cudaStream_t st) {
+    if (f.n == 0) return cudaSuccess;
+    finalize_kernel<<<(f.n + 255) / 256, 256, 0, st>>>(f);
     return cudaGetLastError();
 }
 

@@ -92,9 +92,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     if (s != HEXO_OK) return s;
     const uint32_t n_out = bp.n_out;
     db.grid = std::max<uint32_t>(1, std::min<uint32_t>(ctx->sm_count * db.ctas_per_sm, (uint32_t)bp.tiles.size()));
-    // one private copy of the sums per CTA, within a 256 MiB budget
-    const uint64_t per_slot = std::max<uint64_t>(1, (uint64_t)n_out * kLimbs * sizeof(unsigned long long));
-    db.n_slots = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(db.grid, (256ull << 20) / per_slot));
+    db.n_slots = std::max<uint32_t>(1, std::min<uint32_t>(db.grid, kSumSlots));   // private copies of the sums
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align_up(off + bytes, 256); return o; };
     const size_t o_sets = take(bp.sets.size() * sizeof(SetDesc));
@@ -105,6 +103,8 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_paths = take(n_out * sizeof(uint64_t));
     const size_t o_disc = take(n_out * sizeof(double));
     const size_t o_pexp = take(n_out * sizeof(int32_t));
+    const bool carried = db.carry != nullptr;   // the serving loop's split requests
+    const size_t o_carry = take(carried ? n_out * sizeof(uint64_t) : 0);
     const size_t o_acc = take((size_t)db.n_slots * n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_acc_sum = take((size_t)n_out * kLimbs * sizeof(unsigned long long));
     const size_t o_price = take(n_out * sizeof(double));
@@ -157,6 +157,7 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
     db.d_disc = reinterpret_cast<double *>(d + o_disc);
     db.d_pexp = reinterpret_cast<int32_t *>(d + o_pexp);
+    db.d_carry_row = carried ? reinterpret_cast<uint64_t *>(d + o_carry) : nullptr;
     db.d_price = reinterpret_cast<double *>(d + o_price);
     db.d_se = reinterpret_cast<double *>(d + o_se);
 
@@ -172,7 +173,8 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
         (e = up(o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(TileDesc))) != cudaSuccess ||
         (e = up(o_paths, bp.opt_paths.data(), n_out * sizeof(uint64_t))) != cudaSuccess ||
         (e = up(o_disc, bp.opt_disc.data(), n_out * sizeof(double))) != cudaSuccess ||
-        (e = up(o_pexp, bp.opt_pexp.data(), n_out * sizeof(int32_t))) != cudaSuccess)
+        (e = up(o_pexp, bp.opt_pexp.data(), n_out * sizeof(int32_t))) != cudaSuccess ||
+        (carried && (e = up(o_carry, bp.opt_carry.data(), n_out * sizeof(uint64_t))) != cudaSuccess))
         return cuda_fail(ctx, e, "upload batch");
     e = cudaStreamSynchronize(st);   // the host vectors are pageable: finish before they can change
     if (e != cudaSuccess) return cuda_fail(ctx, e, "upload batch");
@@ -202,10 +204,22 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
     if (db.args.n_tiles > 0)
         if ((e = launch_paths(db.f32, db.plan.shape, db.grid, db.smem, st, db.args)) != cudaSuccess) return e;
     if ((e = cudaEventRecordWithFlags(db.ev_k1, st, rec_flags)) != cudaSuccess) return e;
-    if ((e = launch_finalize(db.args.acc, db.n_slots, db.args.acc_slot_stride, db.d_paths, db.d_disc, db.d_pexp,
-                             n_out, db.d_price, db.d_se, db.d_acc_sum, st, db.d_cv_eg, db.d_cv_partner)) !=
-        cudaSuccess)
-        return e;
+    FinalizeArgs fa;
+    fa.acc = db.args.acc;
+    fa.n_slots = db.n_slots;
+    fa.slot_stride = db.args.acc_slot_stride;
+    fa.n_paths = db.d_paths;
+    fa.disc = db.d_disc;
+    fa.pay_exp = db.d_pexp;
+    fa.n = n_out;
+    fa.price = db.d_price;
+    fa.se = db.d_se;
+    fa.acc_sum = db.d_acc_sum;
+    fa.cv_eg = db.d_cv_eg;
+    fa.cv_partner = db.d_cv_partner;
+    fa.carry = db.carry;
+    fa.carry_row = db.d_carry_row;
+    if ((e = launch_finalize(fa, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_price, db.d_price, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(db.h_se, db.d_se, n_out * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if (copy_acc)

@@ -32,12 +32,24 @@ cudaError_t launch_paths(bool f32, const LaunchShape &sh, uint32_t grid, size_t 
 // caller's launch shape never lowers the limit under another's launch.
 cudaError_t paths_smem_limit(const void *fn, int dev);
 
-// Finaliser: sums the n_slots private copies of the limbs (acc_sum, when not
-// null, receives the totals) and writes price and standard error per slot.
-cudaError_t launch_finalize(const unsigned long long *acc, uint32_t n_slots, uint64_t slot_stride,
-                            const uint64_t *n_paths, const double *disc, const int32_t *pay_exp, uint32_t n,
-                            double *price, double *se, unsigned long long *acc_sum, cudaStream_t st,
-                            const double *cv_eg = nullptr, const uint32_t *cv_partner = nullptr);
+// Finaliser: sums the n_slots private copies of the limbs and writes price
+// and standard error per output slot.
+struct FinalizeArgs {
+    const unsigned long long *acc = nullptr;   // [slot * slot_stride + out * kLimbs + limb]
+    uint32_t n_slots = 1;
+    uint64_t slot_stride = 0;
+    const uint64_t *n_paths = nullptr;         // per output: paths that price it
+    const double *disc = nullptr;              // per output: exp(-r T)
+    const int32_t *pay_exp = nullptr;          // per output: E, payoffs summed in units of 2^E
+    uint32_t n = 0;                            // outputs
+    double *price = nullptr, *se = nullptr;
+    unsigned long long *acc_sum = nullptr;     // optional: the totals of this launch
+    const double *cv_eg = nullptr;             // optional control variate: E[(G - K)^+] per output
+    const uint32_t *cv_partner = nullptr;      //   and the slot of its geometric sums (~0 elsewhere)
+    unsigned long long *carry = nullptr;       // optional: running sums of requests split across launches
+    const uint64_t *carry_row = nullptr;       //   per output: (row << 1) | last block, ~0 = not carried
+};
+cudaError_t launch_finalize(const FinalizeArgs &f, cudaStream_t st);
 // The geometric control variate's analytic part for a planned batch:
 // E[(G - K)^+] per control-variate option into *eg and its geometric-sum slot
 // into *partner (device arrays of n_out entries, allocated here).

@@ -325,10 +325,19 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     if (e == cudaSuccess && n_tiles > 0) e = launch_paths(f32, sh, grid, paths_smem_bytes(kNaBlock, 1), s, a);
     double *d_price = reinterpret_cast<double *>(base + kOffPrice);
     double *d_se = reinterpret_cast<double *>(base + kOffSe);
-    if (e == cudaSuccess)
-        e = launch_finalize(a.acc, 1, a.acc_slot_stride, reinterpret_cast<const uint64_t *>(base + kOffPaths),
-                            reinterpret_cast<const double *>(base + kOffDisc),
-                            reinterpret_cast<const int32_t *>(base + kOffPexp), n_opts, d_price, d_se, nullptr, s);
+    if (e == cudaSuccess) {
+        FinalizeArgs fa;
+        fa.acc = a.acc;
+        fa.n_slots = 1;
+        fa.slot_stride = a.acc_slot_stride;
+        fa.n_paths = reinterpret_cast<const uint64_t *>(base + kOffPaths);
+        fa.disc = reinterpret_cast<const double *>(base + kOffDisc);
+        fa.pay_exp = reinterpret_cast<const int32_t *>(base + kOffPexp);
+        fa.n = n_opts;
+        fa.price = d_price;
+        fa.se = d_se;
+        e = launch_finalize(fa, s);
+    }
     uint32_t ctl[2] = {0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(price_out, d_price, n_opts * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && stderr_out)

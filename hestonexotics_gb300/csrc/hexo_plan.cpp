@@ -231,6 +231,7 @@ void batch_add(BatchPlan &b, const SetPlan &sp, uint32_t out_base, uint32_t cv_b
         b.opt_paths.resize(n_out_end, 0);
         b.opt_disc.resize(n_out_end, 1.0);
         b.opt_pexp.resize(n_out_end, 0);
+        b.opt_carry.resize(n_out_end, ~0ull);
     }
     for (size_t i = 0; i < sp.opts.size(); ++i) {
         const uint32_t o = global(sp.opts[i].out_index);

@@ -56,6 +56,8 @@ struct BatchPlan {
     std::vector<uint64_t> opt_paths;    // per output slot: paths that price it
     std::vector<double> opt_disc;       // per output slot: exp(-r T)
     std::vector<int32_t> opt_pexp;      // per output slot: E, payoffs summed in units of 2^E
+    std::vector<uint64_t> opt_carry;    // per output slot: (row << 1) | last block of a request whose sums
+                                        // are carried across launches (the serving loop); ~0 = none
     uint32_t n_out = 0;                 // output slots: the requests' options, then the control variate's
     std::vector<hexo_params> set_params;
     struct CvLeader {                   // an Asian option priced with the geometric control variate

@@ -48,6 +48,8 @@ struct DeviceBatch {
     uint64_t *d_paths = nullptr;
     double *d_disc = nullptr, *d_price = nullptr, *d_se = nullptr;
     int32_t *d_pexp = nullptr;       // per output slot: E, payoffs summed in units of 2^E
+    unsigned long long *carry = nullptr;   // running sums of split requests (the server's pool), or null
+    uint64_t *d_carry_row = nullptr;       // per output slot: (row << 1) | last block, ~0 = not carried
     double *h_price = nullptr, *h_se = nullptr;
     unsigned long long *h_acc = nullptr;
     double *d_cv_eg = nullptr;         // control variate: E[(G - K)^+] per output slot (NaN elsewhere)

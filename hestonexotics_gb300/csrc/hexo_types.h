@@ -40,6 +40,10 @@ constexpr uint32_t kWarpScratchBytes = kConvQueue * 2; // per warp: the queue
 // per launch control block: tile queue head (u32), error flags (u32), exponential-branch steps (u64)
 constexpr size_t kCtlBytes = 16;
 constexpr int kRingSlots = 3;        // per path: normal buffer, uniform buffer, one look-ahead block
+// Private copies of a launch's payoff sums: CTA b adds into copy b % kSumSlots,
+// so few CTAs share an address while the copies' memory and traffic stay
+// small (n_options * 48 bytes each)
+constexpr uint32_t kSumSlots = 16;
 
 struct SegDesc {
     // FP64 constants of one step width dt (HSimulation.tpp:55-79, hoisted)

@@ -153,10 +153,10 @@ class Server:
     until that request is priced and returns its (price, stderr) arrays."""
 
     def __init__(self, engine: "Engine", cfg: Config, mem_cap_bytes: int = 0, max_batch_requests: int = 0,
-                 max_inflight: int = 0):
+                 max_inflight: int = 0, launch_path_steps: int = 0):
         self.engine = engine
         self._lib = engine._lib
-        opts = L.hexo_server_opts(cfg.c(), mem_cap_bytes, max_batch_requests, max_inflight)
+        opts = L.hexo_server_opts(cfg.c(), mem_cap_bytes, max_batch_requests, max_inflight, launch_path_steps)
         self.handle = C.c_void_p()
         engine._check(self._lib.hexo_server_create(engine._ctx, C.byref(opts), C.byref(self.handle)))
         self._pending = {}   # ticket -> (keep-alive objects, outputs)

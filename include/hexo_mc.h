@@ -222,14 +222,24 @@ hexo_status hexo_batch_destroy(hexo_batch *b);
 /* A continuous-batching pricing server on one context.  No counterpart in
  * the reference (whose only pricing call is the blocking HSimulation::price,
  * src/inc/HSimulation.h:44-96); it exists so that a calibration or quoting
- * service can keep many small requests in flight at once.  Requests are
- * admitted first come, first served while the device memory of the launches
- * in flight stays under mem_cap_bytes; every admitted request joins the next
- * persistent launch, and up to max_inflight launches run at once, each on
- * its own stream.  A request's prices do not depend on what it was batched
- * with: path k of a request always draws from RNG(16, seed + k), and sums are
- * exact integers, so results equal those of hexo_price_batch for the request
- * alone, bit for bit. */
+ * service can keep many small requests in flight at once.
+ *
+ * A request runs as one or more blocks of consecutive paths, each in a
+ * persistent launch shared with the blocks of other requests; its exact
+ * payoff sums stay in a device pool between launches, and the launch with its
+ * last block finalises it.  Each launch takes one block from each admitted
+ * request without a block in flight, those that have had the fewest blocks
+ * first, sized so that the launch holds about launch_path_steps of work: a
+ * large request no longer holds the device while small ones wait.  Requests
+ * are admitted first come, first served while their running sums fit the
+ * pool (a quarter of the cap, at most 64 MiB), and one that does not fit yet
+ * lets later ones pass for at most 50 ms; launches run while the device
+ * memory of those in flight stays under mem_cap_bytes, up to max_inflight at
+ * once, each on its own stream.  Path k of a request always draws from the
+ * stream seeded {seed + k, stream, 0, 0} and sums are exact integers, so a
+ * request's prices equal those of hexo_price_batch for the request alone,
+ * bit for bit, whatever it was batched with and however it was split.  With
+ * the geometric control variate a request runs as one block. */
 typedef struct hexo_server hexo_server;
 
 typedef struct hexo_server_opts {
@@ -237,13 +247,16 @@ typedef struct hexo_server_opts {
     uint64_t mem_cap_bytes;        /* device memory of launches in flight; 0 = the context's cap */
     uint32_t max_batch_requests;   /* requests per launch; 0 = 64 */
     uint32_t max_inflight;         /* launches in flight (streams); 0 = 2, at most 16 */
+    uint64_t launch_path_steps;    /* work of one launch, in path-steps; blocks are cut to it; 0 = 2^30
+                                      (about 25 ms on a GB300); UINT64_MAX = never split a request */
 } hexo_server_opts;
 
 typedef struct hexo_server_stats {
     uint64_t submitted, admitted, completed, failed;
     uint64_t batches;              /* launches made */
+    uint64_t chunks;               /* request blocks launched (a request split in k blocks counts k) */
     uint64_t queued_now, queued_max, inflight_now;
-    uint64_t mem_in_use, mem_peak; /* admitted device bytes (planner estimate) */
+    uint64_t mem_in_use, mem_peak; /* device bytes: the pool of running sums and the launches in flight */
     uint64_t nominal_path_steps;   /* of completed requests */
     double busy_seconds;           /* wall time with at least one launch in flight */
     double p50_ms, p99_ms, mean_ms;/* submit-to-completion latency of completed requests */

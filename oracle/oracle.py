@@ -254,3 +254,26 @@ def heston_chf_grad(params5, tau, u: complex) -> np.ndarray:
     out = np.zeros(12)
     lib().oracle_heston_chf_grad(_p(p), C.c_double(tau), C.c_double(u.real), C.c_double(u.imag), _p(out))
     return out[0::2] + 1j * out[1::2]
+
+
+# ------------------------------------------------------------ work counts
+
+def nominal_path_steps(T, n_paths, *, step_mode=1, steps=252, steps_per_year=252.0) -> int:
+    """Nominal path-steps of one request, counted as the reference walks its
+    time grid (HSimulation.tpp:29-46): a path runs to the last maturity whose
+    options it prices, and reaching maturity T_j takes steps_j grid steps
+    (the `steps` argument per maturity, or max(5, round(steps_per_year T_j)) on
+    the daily grid).  Paths that a later maturity needs count that
+    maturity's steps.  Pure Python: the CPU baseline counts its own work."""
+    T = np.asarray(T, dtype=np.float64)
+    n = np.asarray(n_paths, dtype=np.uint64)
+    uT = np.unique(T)
+    if step_mode == 1:
+        st = np.maximum(5.0, np.rint(steps_per_year * uT)).astype(np.int64)
+    else:
+        st = np.full(len(uT), int(steps), dtype=np.int64)
+    mat_paths = np.array([int(n[T == t].max()) for t in uT], dtype=np.int64)
+    thr = np.zeros(len(uT) + 1, dtype=np.int64)
+    for j in range(len(uT) - 1, -1, -1):           # paths that reach maturity j
+        thr[j] = max(thr[j + 1], mat_paths[j])
+    return int(sum((int(thr[j]) - int(thr[j + 1])) * int(st[j]) for j in range(len(uT))))

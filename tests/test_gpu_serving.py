@@ -1,13 +1,16 @@
 """Serving loop (hexo_server_*): continuous batching must not change results.
 
-A request priced through the server, batched with whatever else is queued,
-gives bit-identical prices and standard errors to the same request priced
-alone with hexo_price_batch (each path draws from its own stream and sums are
-exact integers).  Admission: a request that can never fit the device-memory
-cap fails with HEXO_ERR_ADMISSION; requests that fit only one at a time are
+A request priced through the server, batched with whatever else is queued
+and split into path blocks that run in different launches, gives
+bit-identical prices and standard errors to the same request priced alone
+with hexo_price_batch (each path draws from its own stream, sums are exact
+integers and a request's running sums stay on the device between its
+blocks).  Admission: a request that can never fit the device-memory cap
+fails with HEXO_ERR_ADMISSION; requests that fit only one at a time are
 queued and all complete.
 """
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -37,6 +40,52 @@ def test_mixed_equals_alone(engine, precision):
     assert st["completed"] == len(reqs) and st["failed"] == 0
     assert st["batches"] >= 3
     assert 0 < st["p50_ms"] <= st["p99_ms"]
+
+
+@pytest.mark.parametrize("precision", [E.FP32, E.FP64])
+def test_blocks_across_launches_equal_alone(engine, precision):
+    # a small launch budget cuts every request into several path blocks that
+    # continue across launches (and across the server's streams)
+    reqs, cfg = small_requests(n=6, precision=precision)
+    alone = [engine.price_batch([rq], cfg)[0] for rq in reqs]
+    with engine.server(cfg, max_batch_requests=4, max_inflight=3, launch_path_steps=1 << 21) as srv:
+        tickets = [srv.submit(rq) for rq in reqs]
+        got = [srv.wait(t) for t in tickets]
+        st = srv.stats()
+    for (pa, sa), (pm, sm) in zip(alone, got):
+        assert np.array_equal(pa, pm) and np.array_equal(sa, sm)
+    assert st["chunks"] >= 2 * len(reqs) and st["completed"] == len(reqs)
+    # and the same requests, never split: the same bits again
+    with engine.server(cfg, launch_path_steps=(1 << 64) - 1) as srv:
+        whole = [srv.wait(srv.submit(rq)) for rq in reqs]
+        st = srv.stats()
+    assert st["chunks"] == len(reqs)
+    for (pa, sa), (pm, sm) in zip(alone, whole):
+        assert np.array_equal(pa, pm) and np.array_equal(sa, sm)
+
+
+def test_large_request_does_not_hold_small_ones(engine):
+    # one request much larger than the launch budget, then small ones: the
+    # small ones finish in launches that run between the large one's blocks
+    reqs, cfg = small_requests(n=5)
+    big = W.uneven_batch(n_sets=1, seed=12, precision=E.FP32, path_scale=1.0 / 4)[0][0]
+    want_big = engine.price_batch([big], cfg)[0]
+    done_order = []
+    with engine.server(cfg, max_batch_requests=8, max_inflight=2, launch_path_steps=1 << 26) as srv:
+        tb = srv.submit(big)
+        ts = [srv.submit(rq) for rq in reqs]
+        pending = {tb: "big", **{t: k for k, t in enumerate(ts)}}
+        while pending:
+            for t in list(pending):
+                if srv.poll(t):
+                    done_order.append(pending.pop(t))
+            time.sleep(0.0005)
+        st = srv.stats()
+    assert done_order[-1] == "big", done_order
+    assert st["chunks"] > len(reqs) + 1
+    with engine.server(cfg) as srv:
+        p, se = srv.wait(srv.submit(big))
+    assert np.array_equal(p, want_big[0]) and np.array_equal(se, want_big[1])
 
 
 def test_order_and_threads_do_not_matter(engine):
