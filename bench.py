@@ -480,9 +480,17 @@ def run_engine(args, rank, world, local):
     from hestonexotics_gb300 import workloads as W
 
     torch.cuda.set_device(local)
-    if args.precision_sweep or args.autotune or args.swift or args.configs:
+    if args.precision_sweep or args.autotune or args.swift or args.configs or args.fp64_only:
         eng = Engine(local)
         out = {"metric": METRIC, "unit": UNIT}
+        if args.fp64_only:
+            reqs, cfg = W.uneven_batch(seed=2, precision=FP64, path_scale=args.path_scale)
+            stream = torch.cuda.ExternalStream(eng.stream)
+            flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+            nan = [(np.full(len(r.options), np.nan), np.full(len(r.options), np.nan)) for r in reqs]
+            r64 = run_fp64_plain(eng, reqs, cfg, nan, flush, stream)
+            out["fp64_plain"] = {k: v for k, v in r64.items() if not k.startswith("fp32")}
+            out["workload"] = f"{WORKLOAD}_paths_x{args.path_scale:g}"
         if args.precision_sweep:
             out["precision_sweep"] = run_precision_sweep(eng, [1 << k for k in (16, 18, 20, 22, 24)])
         if args.swift:
@@ -501,9 +509,12 @@ def run_engine(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     eng = Engine(local)
-    reqs, cfg = W.uneven_batch(seed=2 + rank, precision=FP32, path_scale=args.path_scale)
-    batch = eng.prepare_batch(reqs, cfg)
+    reqs, cfg = W.uneven_batch(seed=2, precision=FP32, path_scale=args.path_scale)
+    # one GPU: the whole batch; N GPUs: range `rank` of every request's paths on each,
+    # merged by one SUM all-reduce of the exact limb sums per step
+    batch = eng.prepare_batch(reqs, cfg) if world == 1 else eng.prepare_batch_partial(reqs, cfg, rank, world)
     info = batch.info()
+    nominal_batch = plan_stats(reqs, cfg).nominal_path_steps   # the whole batch, all ranks together
     stream = torch.cuda.ExternalStream(eng.stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -522,6 +533,7 @@ def run_engine(args, rank, world, local):
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     step_ms, kernel_ms = [], []
+    merged = None
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()                      # L2 flush between timed launches (not timed)
@@ -529,42 +541,63 @@ def run_engine(args, rank, world, local):
         batch.launch()
         with torch.cuda.stream(stream):
             ev[k][1].record(stream)
-        batch.collect()
-        step_ms.append(ev[k][0].elapsed_time(ev[k][1]))
+        if world == 1:
+            batch.collect()
+            step_ms.append(ev[k][0].elapsed_time(ev[k][1]))
+        else:                                  # the exchange: one SUM all-reduce of every request's limbs
+            import torch.distributed as dist
+            limbs = batch.collect_limbs()
+            t0 = time.perf_counter()
+            tl = torch.from_numpy(limbs.astype(np.int64)).to(f"cuda:{local}")
+            dist.all_reduce(tl, op=dist.ReduceOp.SUM)
+            merged = tl.cpu().numpy().astype(np.uint64)
+            step_ms.append(ev[k][0].elapsed_time(ev[k][1]) + 1e3 * (time.perf_counter() - t0))
         last = batch.info()
         kernel_ms.append(last["last_kernel_ms"])
     p_quad = last["quad_steps"] / max(1, last["executed_path_steps"])   # branch mix the kernel counted
     barrier()
     clk = clocks.stop()
     total_ms = sum(step_ms)
-    nominal = info["nominal_path_steps"]
+    nominal = info["nominal_path_steps"]       # this rank's share
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([total_ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-        n = torch.tensor([float(nominal)], device=f"cuda:{local}")
-        dist.all_reduce(n)
-        nominal_all = float(n.item())
+    value = nominal_batch * args.steps / (total_ms * 1e-3)
+    if world == 1:
+        fp32_outputs = [(p.copy(), s.copy()) for p, s in batch.outputs]
     else:
-        nominal_all = float(nominal)
-    value = nominal_all * args.steps / (total_ms * 1e-3)
-    fp32_outputs = [(p.copy(), s.copy()) for p, s in batch.outputs]
+        from hestonexotics_gb300 import shard as S
+        fp32_outputs = S.finalize_batch(reqs, cfg, merged)
     batch.close()
+
+    # e2e: host buffers through the public call; N GPUs: the sharded batch
+    # (planning, upload, one launch per rank, the limbs' all-reduce, the host finaliser)
+    e2e_s = []
+    for _ in range(max(1, min(args.steps, 2))):
+        barrier()
+        t0 = time.perf_counter()
+        if world == 1:
+            eng.price_batch(reqs, cfg)
+        else:
+            from hestonexotics_gb300 import shard as S
+            S.price_batch_sharded(reqs, cfg, engine=eng)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_t = statistics.median(e2e_s)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_t], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = nominal_batch / e2e_t
 
     result = None
     if rank == 0:
-        # e2e: host buffers through the public batch call
-        e2e_s = []
-        for _ in range(max(1, min(args.steps, 2))):
-            t0 = time.perf_counter()
-            eng.price_batch(reqs, cfg)
-            e2e_s.append(time.perf_counter() - t0)
-        e2e_value = nominal / statistics.median(e2e_s)
-
-        # the plain FP64 form on every set, one request per launch
+        # the plain FP64 form on every set (or the first --fp64-sets), one request per launch
         cfg64 = type(cfg)(**{**cfg.__dict__, "precision": FP64})
-        fp64 = run_fp64_plain(eng, reqs, cfg64, fp32_outputs, flush, stream)
+        n64 = min(args.fp64_sets, len(reqs))
+        fp64 = run_fp64_plain(eng, reqs[:n64], cfg64, fp32_outputs[:n64], flush, stream) if n64 else None
 
         peaks = eng.pipe_peaks()
         kms = statistics.mean(kernel_ms)
@@ -581,11 +614,11 @@ def run_engine(args, rank, world, local):
         if args.serve_rates:
             rates = [float(x) for x in args.serve_rates.split(",") if x]
             serving = run_serving(eng, rates, args.serve_min_requests, args.serve_seconds, args.serve_fp64_requests)
-        cpu = run_cpu_baseline(rank, steps=3)
+        cpu = run_cpu_baseline(rank, steps=args.cpu_baseline_steps) if args.cpu_baseline_steps > 0 else None
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 paths, f32 AS241, exact integer sums, f64 finalise",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32 paths, f32 AS241, exact integer sums, f64 finalise",
             "data": "synthetic (seeded uneven 64-set batch; the reference prices live option chains)",
             "config": workload_config() if args.path_scale == 1.0 else
             {**workload_config(), "workload": f"{WORKLOAD}_paths_x{args.path_scale:g}"},
@@ -593,7 +626,8 @@ def run_engine(args, rank, world, local):
                        "paths": info["n_paths"], "executed_path_steps": info["executed_path_steps"],
                        "tiles": info["n_tiles"], "block": info["block"], "paths_per_thread": info["paths_per_thread"],
                        "unroll": info["unroll"], "grid": info["grid"], "l2": "flushed between timed launches",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": "one GPU" if world == 1 else
+                       f"paths of every request split over {world} GPUs, one SUM all-reduce of the limbs per step"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
                     "d2h_bytes_per_step": info["d2h_bytes"],
                     "what": "hexo_price_batch with host buffers: planning, upload, run, download"},
@@ -607,7 +641,7 @@ def run_engine(args, rank, world, local):
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                            "what": "graph launch of the whole batch"},
             "serving": serving,
-            "cpu_baseline": {k: v for k, v in cpu.items() if k != "nominal_path_steps"},
+            "cpu_baseline": {k: v for k, v in cpu.items() if k != "nominal_path_steps"} if cpu else None,
             "clocks": clk,
             "gpu_launches": args.steps * 2,
             "fp64_plain": {"value": fp64["value"], "e2e": fp64["e2e"], "unit": UNIT, "sets": fp64["sets"],
@@ -615,8 +649,8 @@ def run_engine(args, rank, world, local):
                            "fp32_vs_fp64_max_rel_err": fp64["fp32_vs_fp64_max_rel_err"],
                            "prices_checked": fp64["prices_checked"],
                            "fp32_within_1se_frac": fp64["fp32_within_1se_frac"],
-                           "what": "one request per launch, all sets, full paths; value device-timed, e2e "
-                                   "through hexo_batch_prepare/launch/collect"},
+                           "what": "one request per launch, full paths; value device-timed, e2e "
+                                   "through hexo_batch_prepare/launch/collect"} if fp64 else None,
         }
     eng.close()
     if world > 1:
@@ -644,7 +678,7 @@ def run_reference(args, rank, world):
               f"counted by the oracle), oracle port of the reference loop (-O3 -ffast-math, OpenMP {threads} threads)")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(steps), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference CPU path)",
+            "scaling": "strong", "vs_baseline": None, "dtype": "f64 (reference CPU path)",
             "data": "synthetic (seeded uneven 64-set batch, bounded sample per step)",
             "config": workload_config(), "impl": "reference",
             "cpu_baseline": {"kind": "port", "cores": threads, "sample": sample, "value": value},
@@ -673,6 +707,12 @@ def main():
                          "GPU both forms against the CPU port")
     ap.add_argument("--autotune", action="store_true",
                     help="instead of the benchmark: the launch-shape sweep on the uneven batch (use --path-scale)")
+    ap.add_argument("--fp64-only", action="store_true",
+                    help="instead of the benchmark: the plain FP64 leg alone (every set, one request per launch)")
+    ap.add_argument("--cpu-baseline-steps", type=int, default=3,
+                    help="timed steps of the CPU baseline leg (median; 0 = skip)")
+    ap.add_argument("--fp64-sets", type=int, default=64,
+                    help="sets of the plain FP64 leg (the first ones; 64 = all, 0 = skip)")
     ap.add_argument("--path-scale", type=float, default=1.0,
                     help="scales every path count of the batch (1.0 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()

@@ -155,6 +155,11 @@ PROTOTYPES = {
     "hexo_calib_destroy": (C.c_int, [_P]),
     "hexo_price_partial": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                      C.POINTER(hexo_mc_cfg), C.c_uint64, C.c_uint64, _U64]),
+    "hexo_price_batch_partial": (C.c_int, [_P, C.POINTER(hexo_request), C.c_uint32, C.POINTER(hexo_mc_cfg),
+                                           C.c_uint32, C.c_uint32, _U64]),
+    "hexo_batch_prepare_partial": (C.c_int, [_P, C.POINTER(hexo_request), C.c_uint32, C.POINTER(hexo_mc_cfg),
+                                             C.c_uint32, C.c_uint32, C.POINTER(_P)]),
+    "hexo_batch_collect_limbs": (C.c_int, [_P, _U64]),
     "hexo_finalize_limbs": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,
                                       C.POINTER(hexo_mc_cfg), _U64, _D, _D]),
     "hexo_price_noalloc": (C.c_int, [C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option), C.c_uint32,

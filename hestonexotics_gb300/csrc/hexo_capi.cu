@@ -238,7 +238,8 @@ hexo_status batch_wait(DeviceBatch &db) {
 }
 
 hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg &cfg,
-                          uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans) {
+                          uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans,
+                          uint32_t shard, uint32_t n_shards) {
     if (reqs == nullptr || n_reqs == 0) return ctx_fail(ctx, HEXO_ERR_INVALID, "no requests");
     plans.resize(n_reqs);
     uint32_t out_base = 0, cv_base = 0;
@@ -248,6 +249,13 @@ hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_re
         hexo_status s = plan_set(reqs[r].params, reqs[r].S0, reqs[r].opts, reqs[r].n_opts, cfg, reqs[r].seed,
                                  reqs[r].stream, path_lo, path_hi, plans[r], err);
         if (s != HEXO_OK) return ctx_fail(ctx, s, "request " + std::to_string(r) + ": " + err);
+        if (n_shards > 1) {   // this shard's contiguous range of the request's paths
+            SetPlan &sp = plans[r];
+            const uint64_t n = sp.path_hi, base = n / n_shards, extra = n % n_shards;
+            sp.path_lo = shard * base + std::min<uint64_t>(shard, extra);
+            sp.path_hi = sp.path_lo + base + (shard < extra ? 1 : 0);
+            sp.set.n_paths = sp.path_hi;
+        }
         batch_add(bp, plans[r], out_base, cv_base);
         out_base += reqs[r].n_opts;
         cv_base += 2u * plans[r].n_cv;
@@ -400,22 +408,32 @@ hexo_status hexo_batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t
                                hexo_batch **out) {
     if (!ctx || !cfg || !out) return HEXO_ERR_INVALID;
     *out = nullptr;
+    return batch_prepare(ctx, reqs, n_reqs, cfg, 0, 1, out);
+}
+
+} // extern "C"
+
+namespace hexo {
+
+hexo_status batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                          uint32_t shard, uint32_t n_shards, hexo_batch **out) {
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     hexo_batch *b = new (std::nothrow) hexo_batch();
     if (!b) return HEXO_ERR_NOMEM;
     BatchPlan bp;
     std::vector<SetPlan> plans;
-    hexo_status s = plan_requests(ctx, reqs, n_reqs, *cfg, 0, ~0ull, bp, plans);
+    hexo_status s = plan_requests(ctx, reqs, n_reqs, *cfg, 0, ~0ull, bp, plans, shard, n_shards);
     if (s == HEXO_OK) s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, b->db);
     if (s != HEXO_OK) { delete b; return s; }
     b->reqs.assign(reqs, reqs + n_reqs);
+    b->partial = n_shards > 1;
     // capture one run in a graph
     cudaStream_t st = ctx->stream;
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t e2 = batch_enqueue(b->db, st, false);
+        cudaError_t e2 = batch_enqueue(b->db, st, b->partial);
         e = cudaStreamEndCapture(st, &graph);
         if (e2 != cudaSuccess) e = e2;
     }
@@ -428,6 +446,10 @@ hexo_status hexo_batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t
     *out = b;
     return HEXO_OK;
 }
+
+} // namespace hexo
+
+extern "C" {
 
 hexo_status hexo_batch_launch(hexo_batch *b) {
     if (!b) return HEXO_ERR_INVALID;
@@ -445,7 +467,7 @@ hexo_status hexo_batch_collect(hexo_batch *b) {
     NvtxRange r("hexo_batch_collect");
     hexo_status s = batch_wait(b->db);
     if (s != HEXO_OK) return s;
-    scatter_outputs(b->db, b->reqs.data(), (uint32_t)b->reqs.size());
+    if (!b->partial) scatter_outputs(b->db, b->reqs.data(), (uint32_t)b->reqs.size());
     return HEXO_OK;
 }
 
@@ -509,6 +531,49 @@ hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, c
     if (e != cudaSuccess) return cuda_fail(ctx, e, "partial launch");
     if ((s = batch_wait(db)) != HEXO_OK) return s;
     std::memcpy(limbs_out, db.h_acc, (size_t)n_opts * kLimbs * sizeof(uint64_t));
+    return HEXO_OK;
+}
+
+hexo_status hexo_price_batch_partial(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                                     uint32_t shard, uint32_t n_shards, uint64_t *limbs_out) {
+    if (!ctx || !cfg || !limbs_out || n_shards == 0) return HEXO_ERR_INVALID;
+    if (shard >= n_shards) return ctx_fail(ctx, HEXO_ERR_INVALID, "shard must be below n_shards");
+    if (cfg->control_variate)
+        return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "the control variate is not supported by partial sums");
+    std::lock_guard<std::mutex> lk(ctx->run_mu);
+    cudaSetDevice(ctx->device);
+    NvtxRange call("hexo_price_batch_partial");
+    BatchPlan bp;
+    std::vector<SetPlan> plans;
+    hexo_status s = plan_requests(ctx, reqs, n_reqs, *cfg, 0, ~0ull, bp, plans, shard, n_shards);
+    if (s != HEXO_OK) return s;
+    const uint32_t n_out = bp.n_out;
+    DeviceBatch db;
+    ArenaLoan loan(ctx, db);
+    if ((s = batch_upload(ctx, std::move(bp), cfg->precision == HEXO_FP32, db)) != HEXO_OK) return s;
+    cudaError_t e = batch_enqueue(db, ctx->stream, true);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "partial launch");
+    if ((s = batch_wait(db)) != HEXO_OK) return s;
+    std::memcpy(limbs_out, db.h_acc, (size_t)n_out * kLimbs * sizeof(uint64_t));
+    return HEXO_OK;
+}
+
+hexo_status hexo_batch_prepare_partial(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs,
+                                       const hexo_mc_cfg *cfg, uint32_t shard, uint32_t n_shards, hexo_batch **out) {
+    if (!ctx || !cfg || !out || n_shards == 0) return HEXO_ERR_INVALID;
+    *out = nullptr;
+    if (shard >= n_shards) return ctx_fail(ctx, HEXO_ERR_INVALID, "shard must be below n_shards");
+    if (cfg->control_variate)
+        return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "the control variate is not supported by partial sums");
+    return batch_prepare(ctx, reqs, n_reqs, cfg, shard, n_shards, out);
+}
+
+hexo_status hexo_batch_collect_limbs(hexo_batch *b, uint64_t *limbs_out) {
+    if (!b || !limbs_out) return HEXO_ERR_INVALID;
+    cudaSetDevice(b->db.ctx->device);
+    hexo_status s = batch_wait(b->db);
+    if (s != HEXO_OK) return s;
+    std::memcpy(limbs_out, b->db.h_acc, (size_t)b->db.plan.n_out * kLimbs * sizeof(uint64_t));
     return HEXO_OK;
 }
 

@@ -87,6 +87,7 @@ struct hexo_ctx {
 struct hexo_batch {
     hexo::DeviceBatch db;
     std::vector<hexo_request> reqs;
+    bool partial = false;   // a shard of a batch: limbs only, prices after the merge
 };
 
 namespace hexo {
@@ -140,8 +141,13 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
 cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc);
 hexo_status batch_wait(DeviceBatch &db);
 hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg &cfg,
-                          uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans);
+                          uint64_t path_lo, uint64_t path_hi, BatchPlan &bp, std::vector<SetPlan> &plans,
+                          uint32_t shard = 0, uint32_t n_shards = 1);
 void scatter_outputs(const DeviceBatch &db, const hexo_request *reqs, uint32_t n_reqs);
+// Plans, uploads and captures a batch (shard `shard` of n_shards of every
+// request's paths when n_shards > 1) as a graph.
+hexo_status batch_prepare(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                          uint32_t shard, uint32_t n_shards, hexo_batch **out);
 // Autotune cache: reads ctx->tune_cache (if any) into the context's shapes.
 void tune_load(hexo_ctx *ctx);
 } // namespace hexo

@@ -129,6 +129,13 @@ class Batch:
         self.engine._check(L.load().hexo_batch_collect(self.handle))
         return self.outputs
 
+    def collect_limbs(self) -> np.ndarray:
+        """Waits for the last launch; its exact limb sums, [options of all requests, 6] uint64."""
+        n = sum(len(p) for p, _ in self.outputs)
+        limbs = np.zeros(n * L.HEXO_LIMBS, dtype=np.uint64)
+        self.engine._check(L.load().hexo_batch_collect_limbs(self.handle, _u64p(limbs)))
+        return limbs.reshape(n, L.HEXO_LIMBS)
+
     def info(self) -> dict:
         inf = L.hexo_batch_info()
         self.engine._check(L.load().hexo_batch_info_get(self.handle, C.byref(inf)))
@@ -339,6 +346,27 @@ class Engine:
         keep.append(c)
         h = C.c_void_p()
         self._check(self._lib.hexo_batch_prepare(self._ctx, arr, len(requests), C.byref(c), C.byref(h)))
+        return Batch(self, h, keep, outputs)
+
+    def batch_partial(self, requests: Sequence[Request], cfg: Config, shard: int, n_shards: int) -> np.ndarray:
+        """Shard `shard` of n_shards of a batch (range `shard` of every request's
+        paths) in one launch: limb sums [options of all requests, 6] uint64."""
+        arr, keep, outputs = self._requests(requests)
+        n = sum(len(rq.options) for rq in requests)
+        limbs = np.zeros(n * L.HEXO_LIMBS, dtype=np.uint64)
+        c = cfg.c()
+        self._check(self._lib.hexo_price_batch_partial(self._ctx, arr, len(requests), C.byref(c), int(shard),
+                                                       int(n_shards), _u64p(limbs)))
+        return limbs.reshape(n, L.HEXO_LIMBS)
+
+    def prepare_batch_partial(self, requests: Sequence[Request], cfg: Config, shard: int, n_shards: int) -> Batch:
+        """The same shard as a captured graph; launch, then collect_limbs()."""
+        arr, keep, outputs = self._requests(requests)
+        c = cfg.c()
+        keep.append(c)
+        h = C.c_void_p()
+        self._check(self._lib.hexo_batch_prepare_partial(self._ctx, arr, len(requests), C.byref(c), int(shard),
+                                                         int(n_shards), C.byref(h)))
         return Batch(self, h, keep, outputs)
 
     def server(self, cfg: Config, **kw) -> Server:

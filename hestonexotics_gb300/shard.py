@@ -1,7 +1,7 @@
 """Path-range shards across ranks, merged exactly.
 
-The paths of one request are independent (path k draws only from
-RNG(16, seed + k)), so a request splits into contiguous path ranges, one per
+The paths of one request are independent (path k draws only from the
+stream seeded {seed + k, stream, 0, 0}), so a request splits into contiguous path ranges, one per
 rank, with no exchange during simulation.  Each rank produces the exact
 integer limb sums of its range (``Engine.partial``, hexo_price_partial); a
 single SUM all-reduce of those integers and the host finaliser
@@ -12,7 +12,9 @@ float sums (src/HSimulation.tpp:10-51); the integer limbs are what make the
 split result independent of the number of shards.
 
 The all-reduce is the only collective, one per call, of n_options * 6
-integers.
+integers.  A whole batch shards the same way in one launch per rank
+(``price_batch_sharded``): range `rank` of every request, one all-reduce of
+all requests' limbs.
 """
 from __future__ import annotations
 
@@ -76,5 +78,37 @@ def price_sharded(request: E.Request, cfg: E.Config, *, rank: int | None = None,
     return E.finalize_limbs(request.params, request.S0, request.options, cfg, total)
 
 
-def price_batch_sharded(requests: Sequence[E.Request], cfg: E.Config, **kw):
-    return [price_sharded(rq, cfg, **kw) for rq in requests]
+def finalize_batch(requests: Sequence[E.Request], cfg: E.Config, limbs: np.ndarray):
+    """Prices and standard errors of every request from the batch's merged
+    limbs (options of all requests in order): [(price, stderr)] per request."""
+    out, row = [], 0
+    for rq in requests:
+        n = len(rq.options)
+        out.append(E.finalize_limbs(rq.params, rq.S0, rq.options, cfg, limbs[row:row + n]))
+        row += n
+    return out
+
+
+def price_batch_sharded(requests: Sequence[E.Request], cfg: E.Config, *, rank: int | None = None,
+                        world: int | None = None, batch_partial: Callable | None = None,
+                        engine: E.Engine | None = None, group=None):
+    """Prices a whole batch with every request's paths split over the ranks:
+    each rank runs one persistent launch over range `rank` of every request
+    (``Engine.batch_partial``, hexo_price_batch_partial), then one SUM
+    all-reduce of all requests' limbs and the host finaliser give every rank
+    the prices of one launch on one GPU, bit for bit.  ``batch_partial(requests,
+    cfg, rank, world)`` returns the [options of all requests, 6] uint64 limbs of
+    the rank's share; by default the engine's GPU launch."""
+    import torch.distributed as dist
+    if rank is None or world is None:
+        if dist.is_available() and dist.is_initialized():
+            rank, world = dist.get_rank(group), dist.get_world_size(group)
+        else:
+            rank, world = 0, 1
+    if batch_partial is None:
+        if engine is None:
+            raise ValueError("pass the engine (or a batch_partial function)")
+        batch_partial = engine.batch_partial
+    n = sum(len(rq.options) for rq in requests)
+    limbs = np.ascontiguousarray(batch_partial(requests, cfg, rank, world), dtype=np.uint64).reshape(n, 6)
+    return finalize_batch(requests, cfg, _all_reduce_sum(limbs, group))

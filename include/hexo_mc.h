@@ -355,6 +355,28 @@ hexo_status hexo_calib_destroy(hexo_calib *c);
 hexo_status hexo_price_partial(hexo_ctx *ctx, const hexo_params *p, double S0, const hexo_option *opts,
                                uint32_t n_opts, const hexo_mc_cfg *cfg, uint64_t path_lo, uint64_t path_hi,
                                uint64_t *limbs_out /* n_opts * HEXO_LIMBS */);
+/* Shard `shard` of n_shards of a whole batch, in one persistent launch:
+ * every request's paths [0, n) (n its largest path count) are cut into
+ * n_shards contiguous ranges of sizes differing by at most one, and this
+ * shard simulates range `shard` of every request.  limbs_out receives six
+ * uint64 limbs per option, the requests' options in order (sum of n_opts
+ * rows), as hexo_price_partial gives them.  Adding the limbs of all shards
+ * (one SUM all-reduce) and finalising each request with hexo_finalize_limbs
+ * gives the prices of hexo_price_batch bit for bit.  The reference's
+ * counterpart is the path partition over threads of HSimulation::price
+ * (src/HSimulation.tpp:23-28).  Not with the control variate. */
+hexo_status hexo_price_batch_partial(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs, const hexo_mc_cfg *cfg,
+                                     uint32_t shard, uint32_t n_shards, uint64_t *limbs_out);
+/* The same shard planned and uploaded once as a captured CUDA graph (launch
+ * and collect as any batch); hexo_batch_collect_limbs then copies the last
+ * run's limbs out.  hexo_batch_collect leaves the requests' price arrays
+ * alone for such a batch: its prices exist only after the merge. */
+hexo_status hexo_batch_prepare_partial(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_reqs,
+                                       const hexo_mc_cfg *cfg, uint32_t shard, uint32_t n_shards, hexo_batch **out);
+/* Waits for the last launch of a batch and copies its limb sums (six per
+ * option, requests in order) into limbs_out. */
+hexo_status hexo_batch_collect_limbs(hexo_batch *b, uint64_t *limbs_out);
+
 /* Host-only: prices and standard errors from (merged) limb sums; the same
  * operation sequence as the device finaliser, so results match it bit for bit. */
 hexo_status hexo_finalize_limbs(const hexo_params *p, double S0, const hexo_option *opts, uint32_t n_opts,

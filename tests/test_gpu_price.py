@@ -177,6 +177,25 @@ def test_shards_merge_bit_identical(engine):
     assert np.array_equal(p, p_merge) and np.array_equal(se, se_merge)
 
 
+@pytest.mark.parametrize("n_shards", [2, 3])
+def test_batch_shards_merge_bit_identical(engine, n_shards):
+    # a whole batch split into n_shards launches (range r of every request's
+    # paths in launch r), merged by adding limbs: the prices of one launch
+    from hestonexotics_gb300 import shard as S
+    reqs, cfg = W.uneven_batch(n_sets=5, path_scale=1 / 512, precision=E.FP32)
+    want = engine.price_batch(reqs, cfg)
+    parts = [engine.batch_partial(reqs, cfg, r, n_shards) for r in range(n_shards)]
+    got = S.finalize_batch(reqs, cfg, sum(parts))
+    for (pw, sw), (pg, sg) in zip(want, got):
+        assert np.array_equal(pw, pg) and np.array_equal(sw, sg)
+    # the prepared (graph) form of a shard gives the same limbs, launch after launch
+    b = engine.prepare_batch_partial(reqs, cfg, 1, n_shards)
+    for _ in range(2):
+        b.launch()
+        assert np.array_equal(b.collect_limbs(), parts[1])
+    b.close()
+
+
 def test_limbs_match_oracle_exactly_where_payoffs_do(engine, oracle):
     # FP64 payoffs agree with the oracle to ~1e-16; their fixed-point sums then agree to a few units
     req, cfg = W.plain_asian(n_paths=3000)

@@ -84,3 +84,53 @@ def test_gloo_shards_merge_bit_identical(tmp_path, oracle, world):
                                         n_default=cfg.n_paths, step_mode=cfg.step_mode, steps=cfg.steps,
                                         steps_per_year=cfg.steps_per_year, seed=rq.seed, stream=rq.stream)
     np.testing.assert_allclose(want[0], p_or, rtol=1e-14, atol=1e-14)
+
+
+def _batch():
+    reqs, cfg = W.uneven_batch(n_sets=3, seed=6, precision=E.FP64, path_scale=1.0 / 4096)
+    out = []
+    for rq in reqs:   # a few options each keep the oracle quick
+        o = rq.options
+        k = slice(0, 5)
+        out.append(E.Request(rq.params, rq.S0, E.Options(o.strike[k], o.T[k], o.payoff[k], o.n_paths[k]),
+                             seed=rq.seed, stream=rq.stream))
+    return out, cfg
+
+
+def _oracle_batch_partial(reqs, cfg, rank, world):
+    # range `rank` of every request's paths, as hexo_price_batch_partial cuts them
+    rows = []
+    for rq in reqs:
+        lo, hi = S.shard_range(S.max_paths(rq, cfg), rank, world)
+        rows.append(_oracle_partial(rq, cfg, lo, hi))
+    return np.concatenate(rows)
+
+
+def _batch_rank_main(rank, world, port, out_dir):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        reqs, cfg = _batch()
+        got = S.price_batch_sharded(reqs, cfg, batch_partial=_oracle_batch_partial)
+        np.save(os.path.join(out_dir, f"b{rank}.npy"), np.concatenate([np.stack(x) for x in got], axis=1))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gloo_batch_shards_merge_bit_identical(tmp_path, oracle):
+    import torch.multiprocessing as mp
+    pytest.importorskip("torch.distributed")
+    world = 2
+    mp.start_processes(_batch_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    reqs, cfg = _batch()
+    want = np.concatenate([np.stack(x) for x in S.finalize_batch(reqs, cfg, _oracle_batch_partial(reqs, cfg, 0, 1))],
+                          axis=1)
+    for r in range(world):
+        assert np.array_equal(np.load(tmp_path / f"b{r}.npy"), want), r
+    # one rank's share is range r of every request: the two shares add to the whole
+    a = _oracle_batch_partial(reqs, cfg, 0, 2)
+    b = _oracle_batch_partial(reqs, cfg, 1, 2)
+    assert np.array_equal(a + b, _oracle_batch_partial(reqs, cfg, 0, 1))
