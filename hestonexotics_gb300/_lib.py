@@ -2,24 +2,30 @@
 
 The library is the only compute path: importing works without it, but every
 call raises ``EngineUnavailable`` when libhexo_mc.so has not been built.
+With HEXO_LIB=checks in the environment the bindings load the bounds-checked
+build of the same sources, libhexo_mc_checks.so, instead.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libhexo_mc.so"
+VARIANTS = {"": "libhexo_mc.so", "checks": "libhexo_mc_checks.so"}
+LIB_PATH = Path(__file__).resolve().parent / VARIANTS.get(os.environ.get("HEXO_LIB", ""), "libhexo_mc.so")
 
 HEXO_OK = 0
 HEXO_ERR_TIMEOUT = 5
 HEXO_ERR_NOT_FOUND = 7
 HEXO_ERR_ADMISSION = 8
 HEXO_ERR_SHUTDOWN = 9
+HEXO_ERR_CHECK = 11
 HEXO_LIMBS = 6
 STATUS_NAMES = {
     0: "HEXO_OK", 1: "HEXO_ERR_INVALID", 2: "HEXO_ERR_CUDA", 3: "HEXO_ERR_NOMEM",
     4: "HEXO_ERR_UNSUPPORTED", 5: "HEXO_ERR_TIMEOUT", 6: "HEXO_ERR_NUMERIC",
     7: "HEXO_ERR_NOT_FOUND", 8: "HEXO_ERR_ADMISSION", 9: "HEXO_ERR_SHUTDOWN", 10: "HEXO_ERR_TOO_LARGE",
+    11: "HEXO_ERR_CHECK",
 }
 
 

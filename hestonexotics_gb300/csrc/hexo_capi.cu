@@ -154,6 +154,12 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     a.queue = reinterpret_cast<unsigned int *>(d + o_ctl);
     a.error = reinterpret_cast<int *>(d + o_ctl + sizeof(uint32_t));
     a.exp_steps = reinterpret_cast<unsigned long long *>(d + o_ctl + 2 * sizeof(uint32_t));
+    a.check = reinterpret_cast<unsigned int *>(d + o_ctl + 4 * sizeof(uint32_t));
+    a.n_out = n_out;
+    a.n_sets = (uint32_t)bp.sets.size();
+    a.n_segs = (uint32_t)bp.segs.size();
+    a.n_mats = (uint32_t)bp.mats.size();
+    a.n_opts = (uint32_t)bp.opts.size();
     db.d_paths = reinterpret_cast<uint64_t *>(d + o_paths);
     db.d_disc = reinterpret_cast<double *>(d + o_disc);
     db.d_pexp = reinterpret_cast<int32_t *>(d + o_pexp);
@@ -231,6 +237,10 @@ cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc) {
 hexo_status batch_wait(DeviceBatch &db) {
     cudaError_t e = cudaStreamSynchronize(db.stream);
     if (e != cudaSuccess) return cuda_fail(db.ctx, e, "batch run");
+    if (db.h_ctl[1] & kErrCheck)
+        return ctx_fail(db.ctx, HEXO_ERR_CHECK,
+                        "a bounds check of the path kernel failed: code " + std::to_string(db.h_ctl[4] >> 24) +
+                            ", detail " + std::to_string(db.h_ctl[4] & 0xffffffu));
     if (db.h_ctl[1] != 0u)
         return ctx_fail(db.ctx, HEXO_ERR_NUMERIC,
                         "a payoff was not finite or outside the fixed-point range [0, 2^16 * 2^E), 2^(E-1) <= S0 < 2^E");
@@ -295,6 +305,7 @@ const char *hexo_status_string(hexo_status s) {
     case HEXO_ERR_ADMISSION: return "request exceeds the device-memory cap";
     case HEXO_ERR_SHUTDOWN: return "server shut down";
     case HEXO_ERR_TOO_LARGE: return "request exceeds the no-allocation entry point's limits";
+    case HEXO_ERR_CHECK: return "a bounds check of the checked build failed";
     }
     return "unknown status";
 }

@@ -63,7 +63,7 @@ constexpr size_t kOffAcc = kOffPexp + na_align(kNaMaxOptions * sizeof(int32_t));
 constexpr size_t kOffPrice = kOffAcc + na_align(kNaMaxOptions * kLimbs * sizeof(unsigned long long));
 constexpr size_t kOffSe = kOffPrice + na_align(kNaMaxOptions * sizeof(double));
 constexpr size_t kOffCtl = kOffSe + na_align(kNaMaxOptions * sizeof(double));
-constexpr size_t kNaUsed = kOffCtl + na_align(2 * sizeof(uint32_t));
+constexpr size_t kNaUsed = kOffCtl + na_align(3 * sizeof(uint32_t));   // tile queue head, error flags, check
 static_assert(kNaUsed <= HEXO_NOALLOC_SCRATCH_BYTES, "no-allocation scratch layout exceeds its array");
 
 } // namespace
@@ -306,7 +306,7 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     }
     // sums, queue head and error flags start at zero on every call
     if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffAcc, 0, (size_t)n_opts * kLimbs * sizeof(unsigned long long), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffCtl, 0, 2 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffCtl, 0, 3 * sizeof(uint32_t), s);
     KernelArgs a;
     std::memset(&a, 0, sizeof a);
     a.sets = reinterpret_cast<const SetDesc *>(base + kOffSet);
@@ -320,6 +320,12 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     a.acc_slot_stride = (uint64_t)n_opts * kLimbs;
     a.queue = reinterpret_cast<unsigned int *>(base + kOffCtl);
     a.error = reinterpret_cast<int *>(base + kOffCtl + sizeof(uint32_t));
+    a.check = reinterpret_cast<unsigned int *>(base + kOffCtl + 2 * sizeof(uint32_t));
+    a.n_out = n_opts;
+    a.n_sets = 1;
+    a.n_segs = n_segs;
+    a.n_mats = m;
+    a.n_opts = n_opts;
     const LaunchShape sh{kNaBlock, 1, 1};
     const uint32_t grid = std::max<uint32_t>(1, std::min(slots, n_tiles));
     if (e == cudaSuccess && n_tiles > 0) e = launch_paths(f32, sh, grid, paths_smem_bytes(kNaBlock, 1), s, a);
@@ -345,5 +351,6 @@ extern "C" hexo_status hexo_price_noalloc(const hexo_params *pp, double S0, cons
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, base + kOffCtl, sizeof ctl, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return HEXO_ERR_CUDA;
+    if (ctl[1] & kErrCheck) return HEXO_ERR_CHECK;
     return ctl[1] != 0u ? HEXO_ERR_NUMERIC : HEXO_OK;
 }

@@ -261,6 +261,10 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         ws[p].nrm0 = ring[p].nrm - lane;
         ws[p].tq_i = tq_i_all + warp * kConvQueue;
         ws[p].lane = lane;
+#ifdef HEXO_CHECKS
+        ws[p].error = a.error;
+        ws[p].check = a.check;
+#endif
     }
     __shared__ uint32_t s_tile;
     // this CTA's private copy of the sums: CTAs never contend for one address
@@ -278,8 +282,12 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                 win[w * kWindow * kLimbs + i] = 0u;
             }
             if (v != 0ull) {
-                const OptDesc &O = a.opts[S.opt_begin + base + i / kLimbs];
-                atomicAdd(&acc[(size_t)O.out_index * kLimbs + i % kLimbs], v);
+                const uint32_t oi = S.opt_begin + base + i / kLimbs;
+                if (HEXO_CHECK(oi < a.n_opts, a.error, a.check, kCheckOpt, oi)) {
+                    const OptDesc &O = a.opts[oi];
+                    if (HEXO_CHECK(O.out_index < a.n_out, a.error, a.check, kCheckOut, O.out_index))
+                        atomicAdd(&acc[(size_t)O.out_index * kLimbs + i % kLimbs], v);
+                }
             }
         }
         __syncthreads();
@@ -292,7 +300,11 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
         __syncthreads();
         if (tile >= a.n_tiles) break;
         const TileDesc td = a.tiles[tile];
+        if (!HEXO_CHECK(td.set < a.n_sets, a.error, a.check, kCheckSet, tile)) continue;   // CTA-uniform skips
         const SetDesc &S = a.sets[td.set];
+        if (!HEXO_CHECK((uint64_t)S.seg_begin + td.seg_count <= a.n_segs && td.seg_count <= S.seg_count, a.error,
+                        a.check, kCheckSegs, td.set))
+            continue;
         const double theta = S.theta;
         const float S0f = S.f_S0, rf = S.f_r;
         uint32_t win_base = 0;   // first set option of the staging window
@@ -343,7 +355,12 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                 }
             }
             for (uint32_t mj = sg.mat_begin; mj < sg.mat_end; ++mj) {
+                if (!HEXO_CHECK(S.mat_begin + mj < a.n_mats && mj < S.mat_count, a.error, a.check, kCheckMat, mj))
+                    continue;
                 const MatDesc M = a.mats[S.mat_begin + mj];
+                if (!HEXO_CHECK(M.opt_end <= S.opt_count && (uint64_t)S.opt_begin + M.opt_end <= a.n_opts, a.error,
+                                a.check, kCheckOpt, M.opt_end))
+                    continue;
                 R asian[PPT], euro[PPT], geo[PPT];
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
@@ -380,6 +397,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
                         flush(S, win_base);
                         win_base = oi - oi % kWindow;
                     }
+                    if (!HEXO_CHECK(oi - win_base < kWindow, a.error, a.check, kCheckWindow, oi - win_base)) continue;
                     fold_option<kF32, PPT, kCV>(a, S, oi, wwin + (oi - win_base) * kLimbs, lane, active, kpath, asian,
                                                 euro, geo);
                 }

@@ -16,7 +16,8 @@
 namespace hexo {
 
 void tune_load(hexo_ctx *ctx) {
-    // defaults; see the tuning record in profiles/ for how they were chosen
+    // defaults: the sweep's fastest shape for both forms on the uneven 64-set batch (256 threads, one
+    // path each, no unrolling; two CTAs per SM, which registers and shared memory both allow)
     ctx->shape_f64 = LaunchShape{256, 1, 1};
     ctx->shape_f32 = LaunchShape{256, 1, 1};
     if (ctx->tune_cache.empty()) return;

@@ -37,8 +37,9 @@ inline int pay_exponent(double S0) {
 constexpr int kRngWords = 16;        // words per RNG buffer (one SHISHUA block)
 constexpr uint32_t kConvQueue = 96;                    // per warp: queued conversion items
 constexpr uint32_t kWarpScratchBytes = kConvQueue * 2; // per warp: the queue
-// per launch control block: tile queue head (u32), error flags (u32), exponential-branch steps (u64)
-constexpr size_t kCtlBytes = 16;
+// per launch control block: tile queue head (u32), error flags (u32), exponential-branch steps (u64),
+// the first failed bounds check (u32, checked builds), padding (u32)
+constexpr size_t kCtlBytes = 24;
 constexpr int kRingSlots = 3;        // per path: normal buffer, uniform buffer, one look-ahead block
 // Private copies of a launch's payoff sums: CTA b adds into copy b % kSumSlots,
 // so few CTAs share an address while the copies' memory and traffic stay
@@ -128,7 +129,24 @@ struct KernelArgs {
     double *dbg_euro;
     uint64_t dbg_lo;
     uint32_t dbg_mats;
-    uint32_t pad2;
+    uint32_t n_out;          // output slots: out_index < n_out
+    uint32_t n_sets, n_segs, n_mats, n_opts;   // descriptor counts, for the bounds-checked build
+    unsigned int *check;     // bounds-checked build: the first failed check, (code << 24) | detail, or null
 };
+
+// Bounds checks of the HEXO_CHECKS build (compiled out otherwise): a failed
+// check sets error bit 2 and records its code and a detail (the offending
+// index, cut to 24 bits) in *check, and the kernel skips the access.
+enum CheckCode : uint32_t {
+    kCheckSet = 1,        // a tile's set index >= n_sets
+    kCheckSegs = 2,       // a set's segment range beyond n_segs
+    kCheckMat = 3,        // a maturity index >= n_mats
+    kCheckOpt = 4,        // an option index >= n_opts or beyond its set
+    kCheckOut = 5,        // an option's out_index >= n_out
+    kCheckWindow = 6,     // a payoff-window offset >= kWindow
+    kCheckQueue = 7,      // a conversion-queue index >= kConvQueue
+    kCheckRing = 8,       // a ring slot other than 0 or 1
+};
+constexpr uint32_t kErrCheck = 4u;   // error bit of a failed bounds check
 
 } // namespace hexo

@@ -71,7 +71,8 @@ typedef enum hexo_status {
     HEXO_ERR_NOT_FOUND = 7,    /* unknown ticket */
     HEXO_ERR_ADMISSION = 8,    /* request can never fit the device-memory cap */
     HEXO_ERR_SHUTDOWN = 9,     /* server is shutting down */
-    HEXO_ERR_TOO_LARGE = 10    /* request exceeds the fixed limits of hexo_price_noalloc */
+    HEXO_ERR_TOO_LARGE = 10,   /* request exceeds the fixed limits of hexo_price_noalloc */
+    HEXO_ERR_CHECK = 11        /* a bounds check of the checked build (libhexo_mc_checks.so) failed */
 } hexo_status;
 
 const char *hexo_status_string(hexo_status s);

@@ -35,7 +35,10 @@ import numpy as np
 os.environ["OMP_NUM_THREADS"] = "1"
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF = Path("/root/reference/src")
+sys.path.insert(0, str(ROOT))
+from hestonexotics_gb300.build import reference_src  # noqa: E402
+
+REF = reference_src()   # HEXO_REFERENCE_SRC, or the checkout beside the repository
 
 
 def P(a):
@@ -91,15 +94,13 @@ def swift_golden():
 
 
 def main():
-    if not (REF / "RNG.cpp").exists():
-        print("reference checkout not found; nothing to do", file=sys.stderr)
+    if REF is None:
+        print("reference checkout not found (set HEXO_REFERENCE_SRC to its src/); nothing to do", file=sys.stderr)
         return 1
     swift_golden()
     if sys.argv[1:] == ["swift"]:
         return 0
-        print("reference checkout not found; nothing to do", file=sys.stderr)
-        return 1
-    subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref"], check=True)
+    subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref", f"REF_SRC={REF}"], check=True)
     lib = C.CDLL(str(ROOT / "oracle" / "_ref" / "libhexo_ref.so"))
 
     # 1. RNG draws

@@ -19,7 +19,13 @@ from hestonexotics_gb300 import engine as E
 
 SRC = ROOT / "tests" / "compat" / "shim_main.cpp"
 LIBDIR = ROOT / "hestonexotics_gb300"
-REF_INC = Path(os.environ.get("HEXO_REFERENCE_INC", "/root/reference/src/inc"))
+def _ref_inc() -> Path:
+    from hestonexotics_gb300.build import reference_src
+    src = reference_src()   # HEXO_REFERENCE_SRC, or the checkout beside the repository
+    return src / "inc" if src is not None else Path("/nonexistent")
+
+
+REF_INC = _ref_inc()
 
 
 def _build(out: Path, extra):
