@@ -614,6 +614,11 @@ def run_engine(args, rank, world, local):
         if args.serve_rates:
             rates = [float(x) for x in args.serve_rates.split(",") if x]
             serving = run_serving(eng, rates, args.serve_min_requests, args.serve_seconds, args.serve_fp64_requests)
+        sweep = None
+        if args.sweep_paths:   # the chain and the Feller-violating set, FP32 against FP64
+            rows = run_precision_sweep(eng, [1 << int(x) for x in args.sweep_paths.split(",") if x])
+            sweep = [{k: r[k] for k in ("set", "paths", "max_rel_err", "max_err_over_se", "within_1se_frac")}
+                     for r in rows]
         cpu = run_cpu_baseline(rank, steps=args.cpu_baseline_steps) if args.cpu_baseline_steps > 0 else None
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -641,6 +646,7 @@ def run_engine(args, rank, world, local):
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                            "what": "graph launch of the whole batch"},
             "serving": serving,
+            "precision_sweep": sweep,
             "cpu_baseline": {k: v for k, v in cpu.items() if k != "nominal_path_steps"} if cpu else None,
             "clocks": clk,
             "gpu_launches": args.steps * 2,
@@ -713,6 +719,8 @@ def main():
                     help="timed steps of the CPU baseline leg (median; 0 = skip)")
     ap.add_argument("--fp64-sets", type=int, default=64,
                     help="sets of the plain FP64 leg (the first ones; 64 = all, 0 = skip)")
+    ap.add_argument("--sweep-paths", default="16,20,24",
+                    help="log2 path counts of the precision sweep in the benchmark line ('' = skip)")
     ap.add_argument("--path-scale", type=float, default=1.0,
                     help="scales every path count of the batch (1.0 = the benchmark workload; smaller for profiling)")
     args = ap.parse_args()

@@ -132,6 +132,7 @@ PROTOTYPES = {
     "hexo_abi_version": (C.c_uint32, []),
     "hexo_ctx_create": (C.c_int, [C.POINTER(_P), C.POINTER(hexo_ctx_opts)]),
     "hexo_ctx_destroy": (C.c_int, [_P]),
+    "hexo_ctx_trim": (C.c_int, [_P]),
     "hexo_ctx_last_error": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
     "hexo_ctx_stream": (_P, [_P]),
     "hexo_mc_cfg_default": (None, [C.POINTER(hexo_mc_cfg)]),

@@ -46,6 +46,26 @@ LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg) {
     return sh;
 }
 
+// A batch with fewer paths than the default shape's CTA slots (2 per SM of
+// 256 threads, one path each) would leave SMs with one CTA and others with
+// two; with narrower CTAs (a multiple of 32 threads, at least 128) the same
+// paths spread over every slot, so the most loaded SM runs fewer warps.
+// Only the default shape is changed (not an explicit or tuned one); the
+// launch shape does not change results.
+void fit_small_batch(hexo_ctx *ctx, const hexo_mc_cfg &cfg, LaunchShape &sh, const std::vector<SetPlan> &plans) {
+    const LaunchShape def{256, 1, 1};
+    const LaunchShape &tuned = cfg.precision == HEXO_FP32 ? ctx->shape_f32 : ctx->shape_f64;
+    if (cfg.block || cfg.paths_per_thread || cfg.unroll || sh.block != def.block || sh.ppt != def.ppt ||
+        tuned.block != def.block || tuned.ppt != def.ppt || tuned.unroll != def.unroll)
+        return;
+    uint64_t paths = 0;
+    for (const SetPlan &sp : plans) paths += sp.path_hi - sp.path_lo;
+    const uint64_t slots = (uint64_t)ctx->sm_count * 2;
+    if (paths == 0 || paths >= slots * def.block) return;
+    const uint64_t per = (paths + slots - 1) / slots;
+    sh.block = (uint32_t)std::max<uint64_t>(128, (per + 31) / 32 * 32);
+}
+
 hexo_status shape_check(hexo_ctx *ctx, bool f32, const LaunchShape &sh, size_t &smem, uint32_t &ctas_per_sm) {
     const void *fn = paths_kernel_ptr(f32, sh.ppt, sh.unroll, sh.cv);
     if (fn == nullptr || sh.block == 0 || sh.block % 32 != 0 || sh.block > 512)
@@ -271,6 +291,7 @@ hexo_status plan_requests(hexo_ctx *ctx, const hexo_request *reqs, uint32_t n_re
         cv_base += 2u * plans[r].n_cv;
     }
     bp.shape = ctx_shape(ctx, cfg);
+    fit_small_batch(ctx, cfg, bp.shape, plans);
     batch_tiles(bp, plans);
     return HEXO_OK;
 }
@@ -358,6 +379,19 @@ hexo_status hexo_ctx_destroy(hexo_ctx *ctx) {
     if (ctx->arena_d) cudaFree(ctx->arena_d);
     if (ctx->arena_h) cudaFreeHost(ctx->arena_h);
     delete ctx;
+    return HEXO_OK;
+}
+
+hexo_status hexo_ctx_trim(hexo_ctx *ctx) {
+    if (!ctx) return HEXO_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->run_mu);
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "hexo_ctx_trim");
+    if (ctx->arena_d) cudaFree(ctx->arena_d);
+    if (ctx->arena_h) cudaFreeHost(ctx->arena_h);
+    ctx->arena_d = ctx->arena_h = nullptr;
+    ctx->arena_dcap = ctx->arena_hcap = 0;
     return HEXO_OK;
 }
 

@@ -91,8 +91,13 @@ struct hexo_batch {
 };
 
 namespace hexo {
+// One-shot memory larger than this is freed at the end of its call instead of
+// being kept for the next one (hexo_ctx_trim frees what is kept).
+constexpr size_t kArenaKeepBytes = 256ull << 20;
+
 // Lends the context's arena to a one-shot batch and keeps whatever larger
-// memory the batch allocated instead (declare after the DeviceBatch).
+// memory the batch allocated instead, up to kArenaKeepBytes (declare after
+// the DeviceBatch; the DeviceBatch frees what is not kept).
 struct ArenaLoan {
     hexo_ctx *ctx;
     DeviceBatch &db;
@@ -102,17 +107,18 @@ struct ArenaLoan {
         db.own_d = db.own_h = false;
     }
     ~ArenaLoan() {
-        if (db.own_d && db.dmem) {
+        if (db.own_d && db.dmem && db.dcap <= kArenaKeepBytes) {
             if (ctx->arena_d) cudaFree(ctx->arena_d);
             ctx->arena_d = db.dmem;
             ctx->arena_dcap = db.dcap;
+            db.own_d = false;
         }
-        if (db.own_h && db.hmem) {
+        if (db.own_h && db.hmem && db.hcap <= kArenaKeepBytes) {
             if (ctx->arena_h) cudaFreeHost(ctx->arena_h);
             ctx->arena_h = db.hmem;
             ctx->arena_hcap = db.hcap;
+            db.own_h = false;
         }
-        db.own_d = db.own_h = false;
     }
     ArenaLoan(const ArenaLoan &) = delete;
     ArenaLoan &operator=(const ArenaLoan &) = delete;
@@ -136,6 +142,8 @@ inline cudaError_t ctx_scratch(hexo_ctx *ctx, size_t bytes, void **p) {
 hexo_status ctx_fail(hexo_ctx *ctx, hexo_status s, const std::string &msg);
 hexo_status cuda_fail(hexo_ctx *ctx, cudaError_t e, const char *what);
 LaunchShape ctx_shape(hexo_ctx *ctx, const hexo_mc_cfg &cfg);
+// Narrows the default launch shape of a batch too small to fill the GPU's CTA slots.
+void fit_small_batch(hexo_ctx *ctx, const hexo_mc_cfg &cfg, LaunchShape &sh, const std::vector<SetPlan> &plans);
 hexo_status shape_check(hexo_ctx *ctx, bool f32, const LaunchShape &sh, size_t &smem, uint32_t &ctas_per_sm);
 hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch &db);
 cudaError_t batch_enqueue(DeviceBatch &db, cudaStream_t st, bool copy_acc);

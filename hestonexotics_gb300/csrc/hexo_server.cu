@@ -362,6 +362,7 @@ bool launch_next(hexo_server *s, std::unique_lock<std::mutex> &lk) {
         cv_base += 2u * b.r->plan.n_cv;
     }
     bp.shape = ctx_shape(s->ctx, s->opts.cfg);
+    fit_small_batch(s->ctx, s->opts.cfg, bp.shape, plans);
     batch_tiles(bp, plans);
     Inflight f;
     f.db.reset(new DeviceBatch());

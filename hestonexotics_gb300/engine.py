@@ -292,6 +292,10 @@ class Engine:
             self._lib.hexo_ctx_destroy(self._ctx)
             self._ctx = C.c_void_p()
 
+    def trim(self):
+        """Frees the device and pinned memory the context keeps between one-shot calls."""
+        self._check(self._lib.hexo_ctx_trim(self._ctx))
+
     def __del__(self):
         try:
             self.close()

@@ -90,12 +90,18 @@ typedef struct hexo_ctx_opts {
 } hexo_ctx_opts;
 
 /* A context keeps the device and pinned host memory of its largest one-shot
- * call (hexo_price, hexo_price_batch, hexo_price_partial) for the next one,
- * so repeated calls allocate nothing; hexo_ctx_destroy frees it. */
+ * call (hexo_price, hexo_price_batch, hexo_price_partial,
+ * hexo_price_batch_partial) for the next one, so repeated calls allocate
+ * nothing, up to 256 MiB of each: a call that needs more frees its memory
+ * when it returns.  hexo_ctx_trim and hexo_ctx_destroy free what is kept.
+ * This memory is the context's own; a server's memory cap does not count it. */
 hexo_status hexo_ctx_create(hexo_ctx **out, const hexo_ctx_opts *opts /* NULL = defaults */);
 /* Waits for the context's work and frees it.  Batches, servers and
  * calibration handles made on the context must be destroyed first. */
 hexo_status hexo_ctx_destroy(hexo_ctx *ctx);
+/* Waits for the context's one-shot calls and frees the device and pinned
+ * host memory it keeps for the next one (the next call allocates again). */
+hexo_status hexo_ctx_trim(hexo_ctx *ctx);
 /* Copies the message of the last failure on this context into buf. */
 hexo_status hexo_ctx_last_error(hexo_ctx *ctx, char *buf, size_t buf_len);
 /* The cudaStream_t (as void*) on which this context launches its kernels. */

@@ -197,3 +197,34 @@ def test_host_finaliser_from_oracle_limbs(lib, oracle):
 def test_abi_version_matches_header_and_bindings(lib):
     m = re.search(r"#define\s+HEXO_ABI_VERSION\s+(\d+)u", HEADER.read_text())
     assert m and int(m.group(1)) == L.ABI_VERSION == lib.hexo_abi_version()
+
+
+def test_checked_build_exports_the_same_functions(lib):
+    from hestonexotics_gb300 import build
+    assert build.LIB_CHECKS.exists()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(build.LIB_CHECKS)], capture_output=True,
+                         text=True).stdout
+    exported = set(re.findall(r"\b(hexo_\w+)\b", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_requests_of_a_workload_never_share_a_path_stream():
+    # path k of a request draws from the stream seeded {seed + k, stream, 0, 0}:
+    # requests with their own stream numbers share none, whatever their seeds
+    import dataclasses
+    reqs, _ = W.uneven_batch(seed=2)
+    assert W.stream_overlaps(reqs) == []
+    arrivals, _ = W.request_stream(500.0, 2.0, seed=3)
+    assert W.stream_overlaps([a.request for a in arrivals]) == []
+    # with the seed word alone, two sets of the benchmark batch shared 2.7M path streams
+    same = [dataclasses.replace(r, stream=0) for r in reqs]
+    assert W.stream_overlaps(same) == [(18, 37, 2723757)] or W.stream_overlaps(same) == [(37, 18, 2723757)]
+
+
+def test_batch_shard_ranges_cover_every_path_once():
+    from hestonexotics_gb300 import shard as S
+    for n in (1, 7, 1000, 4194304, 4194305):
+        for world in (1, 2, 3, 8):
+            spans = [S.shard_range(n, r, world) for r in range(world)]
+            assert spans[0][0] == 0 and spans[-1][1] == n
+            assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))

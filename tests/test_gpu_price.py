@@ -158,11 +158,27 @@ def test_prepared_graph_relaunch(engine):
 
 
 def test_uneven_batch_fp64_vs_oracle(engine, oracle):
-    reqs, cfg = W.uneven_batch(n_sets=3, path_scale=1 / 256, precision=E.FP64)
+    # every one of the benchmark batch's 64 sets (their own parameters, chains,
+    # schedules and stream numbers) at 1/1024 of their paths, against the oracle
+    reqs, cfg = W.uneven_batch(seed=2, path_scale=1 / 1024, precision=E.FP64)
     out = engine.price_batch(reqs, cfg)
-    for rq, (p, _) in zip(reqs, out):
-        op, _, _ = oracle_price(oracle, rq, cfg)
+    for rq, (p, se) in zip(reqs, out):
+        op, ose, _ = oracle_price(oracle, rq, cfg)
         assert_fp64_close(p, op, rq.S0)
+        np.testing.assert_allclose(se, ose, rtol=1e-7, atol=1e-12 * rq.S0)
+
+
+@pytest.mark.parametrize("maker", [W.single_chain, W.feller_violating])
+def test_precision_sweep_fp32_vs_fp64(engine, maker):
+    # the chain (8 maturities x 50 strikes x Asian/European) and the
+    # Feller-violating set at 2^16, 2^20 and 2^24 paths: the FP32 form within
+    # 1e-4 relative of the FP64 form on the same streams (prices above
+    # 1e-3 S0) and inside one FP32 standard error everywhere
+    for n in (1 << 16, 1 << 20, 1 << 24):
+        req, cfg64 = maker(n_paths=n, precision=E.FP64)
+        p64, _ = engine.price(req.params, req.S0, req.options, cfg64)
+        p32, se32 = engine.price(req.params, req.S0, req.options, E.Config(**{**cfg64.__dict__, "precision": E.FP32}))
+        fp32_check(p32, se32, p64, req.S0)
 
 
 def test_shards_merge_bit_identical(engine):
@@ -282,3 +298,31 @@ def test_extreme_spot_levels(engine, oracle):
         p64, _ = engine.price(params, S0, req.options, E.Config(**{**cfg.__dict__}))
         op, _, _ = oracle_price(oracle, req, cfg)
         assert_fp64_close(p64, op, S0)
+
+
+def test_trim_frees_the_kept_memory_and_calls_still_agree(engine):
+    req, cfg = W.single_chain(n_paths=2000)
+    first = engine.price(req.params, req.S0, req.options, cfg)
+    engine.trim()
+    engine.trim()   # nothing kept: a no-op
+    again = engine.price(req.params, req.S0, req.options, cfg)
+    assert np.array_equal(first[0], again[0]) and np.array_equal(first[1], again[1])
+
+
+def test_small_batches_spread_over_every_sm(engine):
+    # 65,536 paths fill 256 CTAs of 256 threads; narrower CTAs spread them over
+    # all 2 x SM slots (same results: the launch shape does not change them)
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    req, cfg = W.plain_asian(n_paths=65536)
+    for prec in (E.FP64, E.FP32):
+        cfg.precision = prec
+        b = engine.prepare_batch([req], cfg)
+        b.launch()
+        (p, se), = b.collect()
+        info = b.info()
+        b.close()
+        per = -(-65536 // (2 * sms))
+        assert info["block"] == max(128, -(-per // 32) * 32) < 256
+        want = engine.price(req.params, req.S0, req.options, E.Config(**{**cfg.__dict__, "block": 256}))
+        assert np.array_equal(p, want[0]) and np.array_equal(se, want[1])
