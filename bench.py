@@ -76,14 +76,14 @@ def alg_ops_per_path_step(p: float) -> dict:
             "mufu": (5.0 - 2.0 * p + n_n) + (1.0 + 2.0 * p + tail) + 1.0 + (1.0 - p + tail) + 2.0,
             "int32_alu": 2.0 * SHISHUA_ALU_PER_WORD}
 
-# DRAM bytes (read + write) of one launch of the FP32 path kernel, from one
-# Nsight Compute capture of this workload at 1/16 of its paths (129.0 MB +
-# 87.3 MB).  The traffic is the CTA-private sum slots a launch touches plus
-# the descriptors; it does not grow with the path count, so it is reported
-# unscaled.
-PATHS_KERNEL_DRAM_BYTES = 129.0e6 + 87.3e6
-PATHS_KERNEL_DRAM_NOTE = ("DRAM bytes per launch from ncu at 1/16 of the paths; sum slots and descriptors, "
-                          "independent of the path count")
+# DRAM bytes (read + write) of one launch of the FP32 path kernel on this
+# workload, from a one-pass Nsight Compute capture of the full batch (30.69 MB
+# read, 0 written, 6.76 s): the 16 private copies of the payoff sums
+# (11.1 MB) and the descriptors the launch reads (19.7 MB, most of them the
+# 1.0M tiles), against 19.9 MB of algorithmic bytes (descriptors and results).
+PATHS_KERNEL_DRAM_BYTES = 30.69e6
+PATHS_KERNEL_DRAM_NOTE = ("DRAM bytes per launch of the full batch, one-pass ncu capture: the 16 private copies "
+                          "of the sums and the descriptors; algorithmic bytes 19.9 MB")
 
 
 def dist_env():
@@ -465,11 +465,42 @@ def run_swift_report(eng, n_sets=1024):
     eng.swift_batch(reqs, grad=True)
     tb = time.perf_counter() - t0
     n_opts = n_sets * len(W.CHAIN_MATURITIES) * 50
+    # the two transforms by direct sums and by FFT at large J: one chain whose
+    # range k2 - k1 fills the 4J the frequencies allow (m raised until it does)
+    prm = W.draw_params(np.random.default_rng(6))
+    K = np.geomspace(60.0, 160.0, 50)
+    transforms = []
+    for J in (1024, 8192, 65536):
+        sp = E.swift_params_dynamic(prm, 1.0, 100.0, K.min(), K.max(), 1e-7)
+        while 2 * (sp["k2"] - sp["k1"] + 1) <= 4 * J:   # finer wavelet scale: a wider k range
+            sp["m"] += 1
+            sp["exp2_m"] *= 2
+            sp["sqrt_exp2_m"] = float(np.sqrt(sp["exp2_m"]))
+            sp["k1"] = int(np.ceil(sp["exp2_m"] * sp["lower"]))
+            sp["k2"] = int(np.floor(sp["exp2_m"] * sp["upper"]))
+        if sp["k2"] - sp["k1"] + 1 > 4 * J:
+            sp["m"] -= 1
+            sp["exp2_m"] //= 2
+            sp["sqrt_exp2_m"] = float(np.sqrt(sp["exp2_m"]))
+            sp["k1"] = int(np.ceil(sp["exp2_m"] * sp["lower"]))
+            sp["k2"] = int(np.floor(sp["exp2_m"] * sp["upper"]))
+        sp["J"] = J
+        row = {"J": J, "k_range": sp["k2"] - sp["k1"] + 1}
+        for name, method in (("direct_ms", 1), ("fft_ms", 2)):
+            eng.swift(prm, 100.0, [(1.0, K)], grad=True, swift_params=[sp], method=method)
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                eng.swift(prm, 100.0, [(1.0, K)], grad=True, swift_params=[sp], method=method)
+                ts.append(time.perf_counter() - t0)
+            row[name] = 1e3 * statistics.median(ts)
+        transforms.append(row)
     return {"calibration_eval": {"chains": 8, "observations": 40, "gpu_ms_prices_and_jacobian": gpu_ms,
                                  "oracle_cpu_ms_1_thread": cpu_ms,
                                  "oracle_note": "direct-sum restatement; the reference uses FFTW and Eigen"},
             "batch": {"sets": n_sets, "chains_per_set": len(W.CHAIN_MATURITIES), "strikes_per_chain": 50,
-                      "seconds": tb, "options_per_s_with_gradients": n_opts / tb}}
+                      "seconds": tb, "options_per_s_with_gradients": n_opts / tb},
+            "transforms_one_chain_50_strikes": transforms}
 
 
 # -------------------------------------------------------------- engine arm

@@ -112,7 +112,7 @@ class hexo_swift_params(C.Structure):
 
 class hexo_swift_chain(C.Structure):
     _fields_ = [("tau", C.c_double), ("strikes", C.POINTER(C.c_double)), ("n", C.c_uint32),
-                ("reserved", C.c_uint32), ("params", C.POINTER(hexo_swift_params)),
+                ("method", C.c_uint32), ("params", C.POINTER(hexo_swift_params)),
                 ("trunc_precision", C.c_double), ("price_out", C.POINTER(C.c_double)),
                 ("grad_out", C.POINTER(C.c_double))]
 

@@ -202,7 +202,12 @@ struct Exp {                 // one expiry of one request
     int32_t k1, k2;
     uint32_t J, n_opt;
     uint64_t tw_off, h_off, v_off, w_off, o_off;  // element offsets into the work buffers
+    uint32_t fft, logN;      // the two transforms by FFT of length N = 2J = 2^logN (else direct sums)
+    uint64_t f_off;          // its two N-element FFT buffers in the FFT workspace
 };
+
+// Expiries with at least this many frequencies use the FFT (automatic method).
+constexpr uint32_t kFftMinJ = 1024;
 
 struct Item {                // 32 consecutive outputs of one expiry
     uint32_t e, first;
@@ -233,9 +238,79 @@ __global__ void tables_kernel(const Exp *ex, const Item *items, uint32_t n_items
     }
 }
 
+// ------------------------------------------------------------------- FFT
+//
+// Both transforms are inverse DFTs of length N = 2J: with w = e^{i pi/(2J)},
+// w^{k(2j+1)} = w^k e^{2 pi i k j / N}, so
+//   V_k = Re(w^k F[k mod N]) sqrt(2^m)/J,  F = IDFT_N(h_0 .. h_{J-1}, 0 .. 0),
+//   c_j = w^{2 k1 j} G[j] sqrt(2^m)/J,     G = IDFT_N(g folded mod N),
+//         g_m = V_{k1+m} w^{k1+m},  m in [0, k2 - k1],
+// IDFT_N(x)[n] = sum_r x_r e^{2 pi i r n / N}.  The IDFT is the radix-2
+// Stockham autosort formulation (Govindaraju et al., "High performance
+// discrete Fourier transforms on graphics processors", SC 2008): log2 N
+// passes, each a butterfly over elements j and j + N/2 whose results land
+// at ((j - k) << 1) + k and that plus Ns, k = j mod Ns, Ns = 2^pass, with
+// twiddle e^{i pi k / Ns}; buffers alternate and the output is in natural
+// order.  O(N log N) instead of the direct sums' O(J (k2 - k1)).
+
+// buffer 0 of an FFT expiry: h_j for j < J, then zeros
+__global__ void fft_load_h_kernel(const Exp *ex, const Item *items, uint32_t n_items, const double2 *h,
+                                  double2 *fbuf) {
+    const uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (it >= n_items) return;
+    const Exp E = ex[items[it].e];
+    const uint32_t m = items[it].first + (threadIdx.x & 31u);
+    if (m >= 2 * E.J) return;
+    fbuf[E.f_off + m] = m < E.J ? h[E.h_off + m] : make_double2(0.0, 0.0);
+}
+
+// buffer 0 of an FFT expiry: the terms V_{k1+m} w^{k1+m} folded mod N
+__global__ void fft_load_g_kernel(const Exp *ex, const Item *items, uint32_t n_items, const double2 *tw,
+                                  const double *V, double2 *fbuf) {
+    const uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (it >= n_items) return;
+    const Exp E = ex[items[it].e];
+    const uint32_t r = items[it].first + (threadIdx.x & 31u), N = 2 * E.J;
+    if (r >= N) return;
+    const uint32_t mask = 4 * E.J - 1, K = (uint32_t)(E.k2 - E.k1 + 1);
+    double re = 0.0, im = 0.0;
+    for (uint32_t m = r; m < K; m += N) {   // K <= 4J = 2N: at most two terms
+        const double v = V[E.v_off + m];
+        const double2 t = tw[E.tw_off + ((uint32_t)(E.k1 + (int32_t)m) & mask)];
+        re = fma(v, t.x, re);
+        im = fma(v, t.y, im);
+    }
+    fbuf[E.f_off + r] = make_double2(re, im);
+}
+
+// one Stockham pass (Ns = 2^pass) of every FFT expiry with more passes to go
+__global__ void fft_pass_kernel(const Exp *ex, const Item *items, uint32_t n_items, uint32_t pass, double2 *fbuf) {
+    const uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (it >= n_items) return;
+    const Exp E = ex[items[it].e];
+    if (pass >= E.logN) return;
+    const uint32_t N = 2 * E.J, half = E.J, j = items[it].first + (threadIdx.x & 31u);
+    if (j >= half) return;
+    const double2 *in = fbuf + E.f_off + (pass & 1u ? N : 0u);
+    double2 *out = fbuf + E.f_off + (pass & 1u ? 0u : N);
+    const uint32_t Ns = 1u << pass, k = j & (Ns - 1u);
+    double s, c;
+    sincospi((double)k / (double)Ns, &s, &c);
+    const double2 a = in[j], b0 = in[j + half];
+    const double2 b = make_double2(b0.x * c - b0.y * s, b0.x * s + b0.y * c);
+    const uint32_t o = ((j - k) << 1) + k;
+    out[o] = make_double2(a.x + b.x, a.y + b.y);
+    out[o + Ns] = make_double2(a.x - b.x, a.y - b.y);
+}
+
+// the result of an FFT expiry's transform (after logN passes)
+__device__ __forceinline__ const double2 *fft_result(const Exp &E, const double2 *fbuf) {
+    return fbuf + E.f_off + (E.logN & 1u ? 2u * E.J : 0u);
+}
+
 // V_k, one lane per k
 __global__ void payoff_kernel(const Exp *ex, const Item *items, uint32_t n_items, const double2 *tw,
-                              const double2 *h, double *V) {
+                              const double2 *h, double *V, const double2 *fbuf) {
     const uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (it >= n_items) return;
     const Exp E = ex[items[it].e];
@@ -243,6 +318,11 @@ __global__ void payoff_kernel(const Exp *ex, const Item *items, uint32_t n_items
     if (k > E.k2) return;
     const uint32_t mask = 4 * E.J - 1;
     const double2 *T = tw + E.tw_off;
+    if (E.fft) {   // Re(w^k F[k mod N])
+        const double2 f = fft_result(E, fbuf)[(uint32_t)k & (2 * E.J - 1)], t = T[(uint32_t)k & mask];
+        V[E.v_off + (uint32_t)(k - E.k1)] = fma(f.x, t.x, -f.y * t.y) * E.sqrt2m / (double)E.J;
+        return;
+    }
     const double2 *Hh = h + E.h_off;
     double acc = 0.0;
     uint32_t idx = (uint32_t)k & mask, step = ((uint32_t)(2 * k)) & mask;   // k (2j + 1) mod 4J
@@ -256,7 +336,7 @@ __global__ void payoff_kernel(const Exp *ex, const Item *items, uint32_t n_items
 
 // c_j and phi(u_j) c_j with its gradient, one lane per j
 __global__ void density_kernel(const Exp *ex, const Item *items, uint32_t n_items, const double2 *tw,
-                               const double *V, double2 *W) {
+                               const double *V, double2 *W, const double2 *fbuf) {
     const uint32_t it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (it >= n_items) return;
     const Exp E = ex[items[it].e];
@@ -264,16 +344,22 @@ __global__ void density_kernel(const Exp *ex, const Item *items, uint32_t n_item
     if (j >= E.J) return;
     const uint32_t mask = 4 * E.J - 1;
     const double2 *T = tw + E.tw_off;
-    const double *Vk = V + E.v_off;
     const uint32_t odd = 2 * j + 1;
-    uint32_t idx = ((uint32_t)E.k1 * odd) & mask;
     double re = 0.0, im = 0.0;
-    for (int32_t k = E.k1; k <= E.k2; ++k) {
-        const double v = Vk[k - E.k1];
-        const double2 t = T[idx];
-        re = fma(v, t.x, re);
-        im = fma(v, t.y, im);
-        idx = (idx + odd) & mask;
+    if (E.fft) {   // w^{2 k1 j} G[j]
+        const double2 g = fft_result(E, fbuf)[j], t = T[((uint32_t)E.k1 * 2u * j) & mask];
+        re = fma(g.x, t.x, -g.y * t.y);
+        im = fma(g.x, t.y, g.y * t.x);
+    } else {
+        const double *Vk = V + E.v_off;
+        uint32_t idx = ((uint32_t)E.k1 * odd) & mask;
+        for (int32_t k = E.k1; k <= E.k2; ++k) {
+            const double v = Vk[k - E.k1];
+            const double2 t = T[idx];
+            re = fma(v, t.x, re);
+            im = fma(v, t.y, im);
+            idx = (idx + odd) & mask;
+        }
     }
     const double sc = E.sqrt2m / (double)E.J;
     const cplx c = C(re * sc, im * sc);
@@ -369,7 +455,8 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
     std::vector<Exp> ex;
     std::vector<double> strikes;
     std::vector<const hexo_swift_chain *> chain_of;
-    uint64_t tw = 0, h = 0, v = 0, w = 0;
+    uint64_t tw = 0, h = 0, v = 0, w = 0, f = 0;
+    uint32_t max_log = 0;
     bool any_grad = false;
     for (uint32_t q = 0; q < n_reqs; ++q) {
         const hexo_swift_request &rq = reqs[q];
@@ -397,7 +484,15 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
             }
             if (!valid_params(sp))
                 return ctx_fail(ctx, HEXO_ERR_UNSUPPORTED, "swift: J must be a power of two up to 65536 with k2 - k1 < 4J");
+            if (ch.method > HEXO_SWIFT_FFT) return ctx_fail(ctx, HEXO_ERR_INVALID, "swift chain: unknown method");
             Exp e{};
+            e.fft = ch.method == HEXO_SWIFT_FFT || (ch.method == HEXO_SWIFT_AUTO && sp.J >= kFftMinJ);
+            if (e.fft) {   // two buffers of N = 2J
+                while ((1u << e.logN) < 2u * sp.J) ++e.logN;
+                e.f_off = f;
+                f += 4ull * sp.J;
+                max_log = std::max(max_log, e.logN);
+            }
             e.p = hp;
             e.tau = ch.tau;
             e.r = rq.params.r;
@@ -422,12 +517,16 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
         }
     }
     if (ex.empty()) return HEXO_OK;
-    std::vector<Item> it_tab, it_pay, it_den, it_pri;
+    std::vector<Item> it_tab, it_pay, it_den, it_pri, it_fn, it_fb;
     for (uint32_t e = 0; e < ex.size(); ++e) {
         for (uint32_t n = 0; n < 4 * ex[e].J; n += 32) it_tab.push_back({e, n});
         for (uint32_t k = 0; k < (uint32_t)(ex[e].k2 - ex[e].k1 + 1); k += 32) it_pay.push_back({e, k});
         for (uint32_t j = 0; j < ex[e].J; j += 32) it_den.push_back({e, j});
         for (uint32_t i = 0; i < ex[e].n_opt; ++i) it_pri.push_back({e, i});
+        if (ex[e].fft) {
+            for (uint32_t n = 0; n < 2 * ex[e].J; n += 32) it_fn.push_back({e, n});   // N elements
+            for (uint32_t j = 0; j < ex[e].J; j += 32) it_fb.push_back({e, j});       // N/2 butterflies
+        }
     }
     const size_t n_opt = strikes.size();
     std::lock_guard<std::mutex> lk(ctx->run_mu);
@@ -443,6 +542,8 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
     const size_t o_tw = take(tw * sizeof(double2)), o_h = take(h * sizeof(double2));
     const size_t o_v = take(v * sizeof(double)), o_w = take(w * sizeof(double2));
     const size_t o_p = take(n_opt * sizeof(double)), o_g = take(any_grad ? n_opt * 5 * sizeof(double) : 0);
+    const size_t o_i5 = take(it_fn.size() * sizeof(Item)), o_i6 = take(it_fb.size() * sizeof(Item));
+    const size_t o_f = take(f * sizeof(double2));
     void *dmem = nullptr;   // the context's arena: no allocation once it is large enough
     cudaError_t err = ctx_scratch(ctx, off, &dmem);
     if (err != cudaSuccess) return cuda_fail(ctx, err, "cudaMalloc swift");
@@ -455,6 +556,8 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
         (err = up(o_i2, it_pay.data(), it_pay.size() * sizeof(Item))) != cudaSuccess ||
         (err = up(o_i3, it_den.data(), it_den.size() * sizeof(Item))) != cudaSuccess ||
         (err = up(o_i4, it_pri.data(), it_pri.size() * sizeof(Item))) != cudaSuccess ||
+        (err = up(o_i5, it_fn.data(), it_fn.size() * sizeof(Item))) != cudaSuccess ||
+        (err = up(o_i6, it_fb.data(), it_fb.size() * sizeof(Item))) != cudaSuccess ||
         (err = up(o_k, strikes.data(), n_opt * sizeof(double))) != cudaSuccess)
         return cuda_fail(ctx, err, "upload swift");
     const Exp *dex = reinterpret_cast<const Exp *>(d + o_ex);
@@ -462,11 +565,26 @@ hexo_status hexo_swift_price(hexo_ctx *ctx, const hexo_swift_request *reqs, uint
     double *dv = reinterpret_cast<double *>(d + o_v);
     double2 *dw = reinterpret_cast<double2 *>(d + o_w);
     double *dp = reinterpret_cast<double *>(d + o_p), *dg = any_grad ? reinterpret_cast<double *>(d + o_g) : nullptr;
+    double2 *df = reinterpret_cast<double2 *>(d + o_f);
     const uint32_t n1 = (uint32_t)it_tab.size(), n2 = (uint32_t)it_pay.size(), n3 = (uint32_t)it_den.size(),
-                   n4 = (uint32_t)it_pri.size();
+                   n4 = (uint32_t)it_pri.size(), n5 = (uint32_t)it_fn.size(), n6 = (uint32_t)it_fb.size();
+    const Item *ifn = reinterpret_cast<const Item *>(d + o_i5), *ifb = reinterpret_cast<const Item *>(d + o_i6);
+    auto fft_passes = [&]() {
+        for (uint32_t pass = 0; pass < max_log; ++pass)
+            fft_pass_kernel<<<(n6 + 3) / 4, 128, 0, st>>>(dex, ifb, n6, pass, df);
+    };
     tables_kernel<<<(n1 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i1), n1, dtw, dh);
-    payoff_kernel<<<(n2 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i2), n2, dtw, dh, dv);
-    density_kernel<<<(n3 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i3), n3, dtw, dv, dw);
+    if (n5) {   // F = IDFT(h) of the FFT expiries
+        fft_load_h_kernel<<<(n5 + 3) / 4, 128, 0, st>>>(dex, ifn, n5, dh, df);
+        fft_passes();
+    }
+    payoff_kernel<<<(n2 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i2), n2, dtw, dh, dv, df);
+    if (n5) {   // G = IDFT(folded V w^k)
+        fft_load_g_kernel<<<(n5 + 3) / 4, 128, 0, st>>>(dex, ifn, n5, dtw, dv, df);
+        fft_passes();
+    }
+    density_kernel<<<(n3 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i3), n3, dtw, dv, dw,
+                                                 df);
     price_kernel<<<(n4 + 3) / 4, 128, 0, st>>>(dex, reinterpret_cast<const Item *>(d + o_i4), n4, dw,
                                                reinterpret_cast<const double *>(d + o_k), dp, dg);
     if ((err = cudaGetLastError()) != cudaSuccess) return cuda_fail(ctx, err, "swift kernels");

@@ -380,15 +380,17 @@ class Engine:
         return Calibration(self, S, r, chains, trunc_precision)
 
     def swift(self, params: Params, S: float, chains, grad: bool = False, swift_params=None,
-              trunc_precision: float = 0.0):
+              trunc_precision: float = 0.0, method: int = 0):
         """SWIFT European call prices (and gradients in v0, theta, rho, kappa,
         sigma) for chains [(tau, strikes), ...]; swift_params: per chain a
         dict / 8-sequence of the reference's SwiftParameters, or None for the
-        reference's dynamic choice.  Returns [price] or [(price, grad[n, 5])]."""
+        reference's dynamic choice; method: 0 automatic, 1 direct sums, 2 FFT.
+        Returns [price] or [(price, grad[n, 5])]."""
         return self.swift_batch([(params, S, chains)], grad, None if swift_params is None else [swift_params],
-                                trunc_precision)[0]
+                                trunc_precision, method)[0]
 
-    def swift_batch(self, requests, grad: bool = False, swift_params=None, trunc_precision: float = 0.0):
+    def swift_batch(self, requests, grad: bool = False, swift_params=None, trunc_precision: float = 0.0,
+                    method: int = 0):
         """requests: [(Params, S, [(tau, strikes), ...]), ...], priced in one call."""
         reqs = (L.hexo_swift_request * len(requests))()
         keep, outs = [], []
@@ -410,6 +412,7 @@ class Engine:
                     keep.append(spc)
                     arr[c].params = C.pointer(spc)
                 arr[c].trunc_precision = trunc_precision
+                arr[c].method = int(method)
                 arr[c].price_out = _dp(price)
                 arr[c].grad_out = _dp(g) if grad else None
                 keep += [K, price, g]

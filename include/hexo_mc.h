@@ -311,10 +311,20 @@ typedef struct hexo_swift_params {
 hexo_status hexo_swift_params_dynamic(const hexo_params *p, double tau, double S, double K_min, double K_max,
                                       double trunc_precision, hexo_swift_params *out);
 
+/* How the two transforms of a chain are evaluated (the reference uses FFTW,
+ * SWIFT.cpp:51-52): direct sums cost O(J (k2 - k1)), the FFT O(J log J);
+ * both give the same prices to rounding. */
+typedef enum hexo_swift_method {
+    HEXO_SWIFT_AUTO = 0,    /* the FFT from J = 1024 frequencies on, direct sums below */
+    HEXO_SWIFT_DIRECT = 1,  /* direct sums */
+    HEXO_SWIFT_FFT = 2      /* radix-2 FFT of length 2J */
+} hexo_swift_method;
+
 typedef struct hexo_swift_chain {
     double tau;                        /* years to expiry */
     const double *strikes;             /* n strikes */
-    uint32_t n, reserved;
+    uint32_t n;
+    uint32_t method;                   /* hexo_swift_method */
     const hexo_swift_params *params;   /* NULL: chosen as hexo_swift_params_dynamic does */
     double trunc_precision;            /* for params == NULL; 0 = 1e-7 */
     double *price_out;                 /* n discounted call prices */

@@ -120,3 +120,40 @@ def test_calibration_recovers_parameters(engine):
     got = _levenberg_marquardt(cal.prices, cal.jacobian, p_true + 0.2, x_obs)
     assert np.abs(got - p_true).sum() < 1e-2, got
     cal.close()
+
+
+@pytest.mark.gpu
+def test_gpu_fft_golden_prices_and_gradients(engine):
+    # the same known answers with both transforms evaluated by the FFT
+    g, p, chains = _golden()
+    out = engine.swift(p, g["S"], chains, grad=True, swift_params=g["swift_params"], method=2)
+    price = np.concatenate([o[0] for o in out])
+    grad = np.concatenate([o[1] for o in out])
+    assert np.sum(np.abs(price - unhex(g["prices"]))) < g["price_tolerance_sum_abs"]
+    want = unhex(g["grad"]).reshape(40, 5)
+    imap = g["grad_index_map"]
+    assert sum(abs(want[i, imap[j]] - grad[i, j]) for i in range(40) for j in range(5)) < g["grad_tolerance_sum_abs"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("J", [1024, 8192, 65536])
+def test_gpu_fft_equals_direct_sums(engine, J):
+    # the dynamic wavelet parameters of random sets with J frequencies: the
+    # FFT (O(J log J)) and the direct sums (O(J (k2 - k1))) give the same
+    # prices and gradients to rounding
+    rng = np.random.default_rng(J)
+    for _ in range(3):
+        p = E.Params(rng.uniform(0.01, 0.09), rng.uniform(0.01, 0.09), rng.uniform(-0.9, -0.1),
+                     rng.uniform(0.5, 5.0), rng.uniform(0.1, 1.0), r=rng.uniform(0.0, 0.05))
+        chains = [(T, np.geomspace(60.0, 160.0, 20)) for T in (0.25, 1.0, 3.0)]
+        sps = []
+        for T, K in chains:
+            sp = E.swift_params_dynamic(p, T, 100.0, K.min(), K.max(), 1e-10)
+            assert sp["k2"] - sp["k1"] + 1 <= 4 * J
+            sp["J"] = J
+            sps.append(sp)
+        direct = engine.swift(p, 100.0, chains, grad=True, swift_params=sps, method=1)
+        fft = engine.swift(p, 100.0, chains, grad=True, swift_params=sps, method=2)
+        for (pd, gd), (pf, gf) in zip(direct, fft):
+            np.testing.assert_allclose(pf, pd, rtol=1e-9, atol=1e-10 * 100.0)
+            np.testing.assert_allclose(gf, gd, rtol=1e-8, atol=1e-9 * 100.0)
