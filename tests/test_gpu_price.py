@@ -326,3 +326,16 @@ def test_small_batches_spread_over_every_sm(engine):
         assert info["block"] == max(128, -(-per // 32) * 32) < 256
         want = engine.price(req.params, req.S0, req.options, E.Config(**{**cfg.__dict__, "block": 256}))
         assert np.array_equal(p, want[0]) and np.array_equal(se, want[1])
+
+
+def test_continue_a_request_with_more_paths(engine):
+    # a request priced on 4,000 paths is continued to 10,000 without
+    # recomputing the first 4,000: the limbs of paths [4000, 10000) add to the
+    # kept limbs, and the sum finalises to the prices of 10,000 paths at once
+    req, cfg = W.single_chain(n_paths=4000)
+    first = engine.partial(req.params, req.S0, req.options, cfg, 0, 4000)
+    more = E.Config(**{**cfg.__dict__, "n_paths": 10000})
+    rest = engine.partial(req.params, req.S0, req.options, more, 4000, 10000)
+    p, se = E.finalize_limbs(req.params, req.S0, req.options, more, first + rest)
+    want = engine.price(req.params, req.S0, req.options, more)
+    assert np.array_equal(p, want[0]) and np.array_equal(se, want[1])
