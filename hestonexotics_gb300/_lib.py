@@ -181,6 +181,7 @@ PROTOTYPES = {
     "hexo_debug_rng_draws": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32,
                                        _D]),
     "hexo_debug_normals": (C.c_int, [_P, _U64, C.c_uint64, _D]),
+    "hexo_debug_as241_check": (C.c_int, [_P, C.c_uint32, C.c_uint64, C.c_uint64, _U64]),
     "hexo_debug_payoff_limbs": (C.c_int, [_P, _D, C.c_uint64, C.c_uint32, C.c_double, C.POINTER(C.c_uint32)]),
     "hexo_debug_pipe_peaks": (C.c_int, [_P, _D]),
     "hexo_debug_path_finals": (C.c_int, [_P, C.POINTER(hexo_params), C.c_double, C.POINTER(hexo_option),

@@ -1,4 +1,5 @@
 // Finaliser, launch dispatch and debug kernels.
+#include <algorithm>
 #include "hexo_device.cuh"
 #include "hexo_final.h"
 #include "hexo_launch.h"
@@ -144,6 +145,29 @@ __global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *ou
     }
 }
 
+// Every float bit pattern b in [lo, hi) through AS241's central branch
+// (branch 0, Q = b) or its tail (branch 1, R = b), once with the kernels'
+// division and root and once with the IEEE intrinsics: counts the results
+// whose bits differ and keeps the smallest such pattern.
+__global__ void dbg_as241_check_kernel(uint32_t branch, uint64_t lo, uint64_t hi, unsigned long long *out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long bad = 0;
+    uint32_t first = 0xffffffffu;
+    for (uint64_t b = lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < hi; b += stride) {
+        const float x = __uint_as_float((uint32_t)b);
+        const float f = branch == 0u ? dev::as241_central<false>(x) : dev::as241_tail<false>(x, false);
+        const float r = branch == 0u ? dev::as241_central<true>(x) : dev::as241_tail<true>(x, false);
+        if (__float_as_uint(f) != __float_as_uint(r)) {
+            ++bad;
+            first = min(first, (uint32_t)b);
+        }
+    }
+    if (bad != 0) {
+        atomicAdd(&out[0], bad);
+        atomicMin(&out[1], (unsigned long long)first);
+    }
+}
+
 __global__ void dbg_limbs_kernel(const double *pay, uint64_t n, bool f32, int E, uint32_t *out) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -171,6 +195,14 @@ cudaError_t launch_dbg_draws(uint32_t seed, uint32_t stream, uint32_t n_streams,
 cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, int E, uint32_t *out, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     dbg_limbs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pay, n, f32, E, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dbg_as241_check(uint32_t branch, uint64_t lo, uint64_t hi, unsigned long long *out,
+                                   cudaStream_t st) {
+    if (hi <= lo) return cudaSuccess;
+    const uint64_t blocks = std::min<uint64_t>((hi - lo + 255) / 256, 152ull * 64);
+    dbg_as241_check_kernel<<<(unsigned)blocks, 256, 0, st>>>(branch, lo, hi, out);
     return cudaGetLastError();
 }
 

@@ -735,6 +735,22 @@ hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n,
     return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug normals");
 }
 
+hexo_status hexo_debug_as241_check(hexo_ctx *ctx, uint32_t branch, uint64_t bits_lo, uint64_t bits_hi,
+                                   uint64_t *out2) {
+    if (!ctx || !out2 || branch > 1u || bits_hi > (1ull << 32) || bits_lo > bits_hi) return HEXO_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->run_mu);
+    cudaSetDevice(ctx->device);
+    DevBuf dout;
+    const unsigned long long init[2] = {0ull, ~0ull};
+    cudaError_t e = dout.alloc(sizeof(init));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dout.p, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_dbg_as241_check(branch, bits_lo, bits_hi, (unsigned long long *)dout.p, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out2, dout.p, sizeof(init), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? HEXO_OK : cuda_fail(ctx, e, "debug AS241 check");
+}
+
 hexo_status hexo_debug_payoff_limbs(hexo_ctx *ctx, const double *pay, uint64_t n, uint32_t precision, double S0,
                                     uint32_t *out) {
     if (!ctx || !pay || !out || n == 0) return HEXO_ERR_INVALID;

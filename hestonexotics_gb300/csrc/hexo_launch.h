@@ -61,6 +61,8 @@ cudaError_t launch_dbg_words(uint32_t seed, uint32_t stream, uint32_t n_streams,
 cudaError_t launch_dbg_draws(uint32_t seed, uint32_t stream, uint32_t n_streams, const uint8_t *kinds, uint32_t n,
                              double *out, cudaStream_t st);
 cudaError_t launch_dbg_normals(const uint64_t *words, uint64_t n, double *out, cudaStream_t st);
+cudaError_t launch_dbg_as241_check(uint32_t branch, uint64_t lo, uint64_t hi, unsigned long long *out,
+                                   cudaStream_t st);
 cudaError_t launch_dbg_limbs(const double *pay, uint64_t n, bool f32, int E, uint32_t *out, cudaStream_t st);
 cudaError_t measure_pipe_peaks(int sm_count, cudaStream_t st, double *out5);
 

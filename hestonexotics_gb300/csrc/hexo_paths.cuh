@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             uint32_t n_exp = 0;
 #pragma unroll
             for (int p = 0; p < PPT; ++p)
-                if (active[p]) n_exp += c[p].u_blocks * (uint32_t)kRngWords + c[p].ucur;
+                if (active[p]) n_exp += c[p].n_u;
             const uint32_t we = __reduce_add_sync(0xffffffffu, n_exp);
             if (lane == 0u && we != 0u) atomicAdd(a.exp_steps, (unsigned long long)we);
         }

@@ -467,6 +467,14 @@ class Engine:
         self._check(self._lib.hexo_debug_normals(self._ctx, _u64p(words), len(words), _dp(out)))
         return out
 
+    def as241_check(self, branch: int, bits_lo: int, bits_hi: int) -> tuple[int, int]:
+        """Float bit patterns in [bits_lo, bits_hi) through AS241's central branch (0) or tail (1) with the
+        kernels' division and root and with the IEEE intrinsics: (number of differing results, smallest
+        differing pattern or 2^64 - 1)."""
+        out = np.zeros(2, dtype=np.uint64)
+        self._check(self._lib.hexo_debug_as241_check(self._ctx, branch, bits_lo, bits_hi, _u64p(out)))
+        return int(out[0]), int(out[1])
+
     def payoff_limbs(self, pay: np.ndarray, precision: int, S0: float = 100.0) -> np.ndarray:
         """The kernels' 25-bit limbs of round(y 2^47) and round(y^2 2^43), y = pay 2^-E with
         2^(E-1) <= S0 < 2^E, [n, 6]."""

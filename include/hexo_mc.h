@@ -480,6 +480,17 @@ hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t stream, 
                                  const uint8_t *kinds, uint32_t n, double *out);
 /* AS241 of u = (double)w / (double)UINT64_MAX for each word: out[i]. */
 hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n, double *out);
+/* Checks the division and square root that the path kernels use inside
+ * AS241 (a reciprocal estimate with Newton and Markstein corrections, in
+ * place of the IEEE intrinsics) on a range of inputs: every float bit
+ * pattern b in [bits_lo, bits_hi), bits_hi <= 2^32, goes through AS241's
+ * central branch (branch 0, Q = b) or its tail (branch 1, R = b) once each
+ * way.  out2[0] receives how many results differ in any bit and out2[1] the
+ * smallest such pattern (UINT64_MAX when none).  No reference counterpart:
+ * it pins the kernels' arithmetic to the reference's IEEE float AS241
+ * (src/as241.f90:88-116). */
+hexo_status hexo_debug_as241_check(hexo_ctx *ctx, uint32_t branch, uint64_t bits_lo, uint64_t bits_hi,
+                                   uint64_t *out2);
 /* The fixed-point split of payoffs as the path kernels fold them for a
  * request with spot S0: for each pay[i] (converted to float first when
  * precision is HEXO_FP32) the six 25-bit limbs out[6*i .. 6*i+5] of

@@ -104,6 +104,24 @@ def test_normals_random_words(engine, oracle):
     assert bad.size == 0, (bad[:5], w[bad[:5]], got[bad[:5]], want[bad[:5]])
 
 
+F32_0425 = 0x3ED9999A   # float(0.425): the largest |Q| of the central branch
+F32_2M54 = 0x24800000   # 2^-54: P - 0.5 = (W - 2^63) 2^-64 with W = (double)w a multiple of 2^10 there
+F32_2M64 = 0x1F800000   # 2^-64: the smallest P, and 1 - P >= 2^-53
+F32_HALF = 0x3F000000
+
+
+def test_as241_division_and_root_on_every_input(engine):
+    """The kernels' AS241 divides and takes its square root with MUFU estimates and Newton/Markstein
+    corrections instead of the IEEE intrinsics.  On every float the central branch can receive
+    (Q = +0, P - 0.5 = 0 rounding to +0, or 2^-54 <= |Q| <= 0.425, both signs) and the tail
+    (2^-64 <= R <= 0.5) the two must agree in every bit."""
+    none = (0, 2 ** 64 - 1)
+    assert engine.as241_check(0, 0, 1) == none
+    for sign in (0, 0x80000000):
+        assert engine.as241_check(0, sign + F32_2M54, sign + F32_0425 + 1) == none
+    assert engine.as241_check(1, F32_2M64, F32_HALF + 1) == none
+
+
 def test_draw_moments_across_streams(engine):
     # moments of the per-path streams the kernels use (RNG(16, seed + k)),
     # 4096 streams x 2048 draws of each kind, within 5 standard errors;
