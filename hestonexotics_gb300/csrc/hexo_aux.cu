@@ -115,13 +115,14 @@ __global__ void dbg_draws_kernel(uint32_t seed, uint32_t stream, uint32_t n_stre
     dev::RngLane c;
     dev::rng_start<true>(g, c, r, ws, seed + k, stream);
     for (uint32_t i = 0; i < n; i += 2) {
-        dev::rng_topup<true>(g, c, r, ws);   // same cadence as one QE step (two draws)
         if (i + 1 < n && kinds[i + 1] == 0) {
             // a QE-shaped pair (normal, normal) or (uniform, normal): the path kernel's draw code
-            const dev::DrawPlan dp = dev::draw_prefetch(c, r);
+            const bool quad = kinds[i] == 0;
+            dev::DrawPlan dp = dev::draw_prefetch(c, r);
+            if (dev::draw_prepare<true>(g, c, r, ws, quad)) dp = dev::draw_prefetch(c, r);
             float z1 = 0.0f, z2;
             uint64_t uw = 0;
-            dev::draw_commit<true>(g, c, r, dp, kinds[i] == 0, z1, uw, z2);
+            dev::draw_commit(g, c, r, dp, quad, z1, uw, z2);
             if (k < n_streams) {
                 out[(size_t)k * n + i] = kinds[i] ? dev::uniform_f64(uw) : (double)z1;
                 out[(size_t)k * n + i + 1] = (double)z2;

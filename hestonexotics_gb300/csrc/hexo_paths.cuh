@@ -48,16 +48,17 @@ struct PathVars {
 // One QE step of one path (HSimulation.tpp:52-86), FP64; returns whether it
 // took the quadratic branch.
 __device__ __forceinline__ bool qe_step(PathVars<false> &pv, const SegDesc &sg, double theta, dev::Shishua &g,
-                                        dev::RngLane &c, const dev::Ring &r) {
-    const dev::DrawPlan dp = dev::draw_prefetch(c, r);
+                                        dev::RngLane &c, const dev::Ring &r, const dev::WarpScratch &ws) {
+    dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const double v = pv.v;
     const double m = __fma_rn(__dsub_rn(v, theta), sg.disc, theta);         // tpp:59
     const double sp2 = fabs(__fma_rn(v, sg.cA, sg.cB));                      // tpp:60
     const double mm = __dmul_rn(m, m);
     const bool quad = sp2 < __dmul_rn(1.5, mm);                              // Psi < PSI_C, tpp:61,63
+    if (dev::draw_prepare<false>(g, c, r, ws, quad)) dp = dev::draw_prefetch(c, r);
     float z1f = 0.0f, z2f;                                                   // draw order, tpp:67,72,80
     uint64_t uw = 0;
-    dev::draw_commit<false>(g, c, r, dp, quad, z1f, uw, z2f);
+    dev::draw_commit(g, c, r, dp, quad, z1f, uw, z2f);
     const double z1 = (double)z1f;
     const double z2 = (double)z2f;
     double vn;
@@ -92,8 +93,9 @@ __device__ __forceinline__ bool qe_step(PathVars<false> &pv, const SegDesc &sg, 
 // reference's tpp:59-60), everything else in float; returns whether it took
 // the quadratic branch.
 __device__ __forceinline__ bool qe_step(PathVars<true> &pv, const SegDesc &sg, dev::Shishua &g, dev::RngLane &c,
-                                        const dev::Ring &r, float S0, float rr, const ds::LogTab *ltab) {
-    const dev::DrawPlan dp = dev::draw_prefetch(c, r);
+                                        const dev::Ring &r, const dev::WarpScratch &ws, float S0, float rr,
+                                        const ds::LogTab *ltab) {
+    dev::DrawPlan dp = dev::draw_prefetch(c, r);
     const ds::F2 v = pv.vd;
     const ds::F2 m = ds::fma(v, ds::F2{sg.ds_disc[0], sg.ds_disc[1]}, ds::F2{sg.ds_m0[0], sg.ds_m0[1]});
     const ds::F2 sp2 = ds::fma(v, ds::F2{sg.ds_cA[0], sg.ds_cA[1]}, ds::F2{sg.ds_cB[0], sg.ds_cB[1]});
@@ -102,9 +104,10 @@ __device__ __forceinline__ bool qe_step(PathVars<true> &pv, const SegDesc &sg, d
     const float t15 = __fmul_rn(1.5f, mm.h);
     const bool quad = fabsf(__fsub_rn(sp2.h, t15)) > __fmul_rn(0x1p-20f, sp2.h) ? sp2.h < t15
                                                                                  : ds::less(sp2, ds::mul_f(mm, 1.5f));
+    if (dev::draw_prepare<true>(g, c, r, ws, quad)) dp = dev::draw_prefetch(c, r);
     float z1 = 0.0f, z2;
     uint64_t uw = 0;
-    dev::draw_commit<true>(g, c, r, dp, quad, z1, uw, z2);
+    dev::draw_commit(g, c, r, dp, quad, z1, uw, z2);
     ds::F2 vn;
     if (quad) {
         const ds::F2 inv = ds::div(ds::F2{__fmul_rn(2.0f, mm.h), __fmul_rn(2.0f, mm.l)}, sp2);   // 2/Psi
@@ -340,9 +343,8 @@ __global__ void __launch_bounds__(512) paths_kernel(const KernelArgs a) {
             for (uint32_t st = 1; st <= sg.n_steps; ++st) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) {
-                    dev::rng_topup<kF32>(g[p], c[p], ring[p], ws[p]);
-                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], S0f, rf, ltab);
-                    else qe_step(pv[p], sg, theta, g[p], c[p], ring[p]);
+                    if constexpr (kF32) qe_step(pv[p], sg, g[p], c[p], ring[p], ws[p], S0f, rf, ltab);
+                    else qe_step(pv[p], sg, theta, g[p], c[p], ring[p], ws[p]);
                     if constexpr (kCV) {
                         yp[p] = yc[p];   // FP32: the exponent of X / S0 that qe_step used
                         if constexpr (kF32) yc[p] = __fmaf_rn(rf, pv[p].v, pv[p].lx);
