@@ -77,11 +77,11 @@ def alg_ops_per_path_step(p: float) -> dict:
             "int32_alu": 2.0 * SHISHUA_ALU_PER_WORD}
 
 # DRAM bytes (read + write) of one launch of the FP32 path kernel on this
-# workload, from a one-pass Nsight Compute capture of the full batch (30.69 MB
-# read, 0 written, 6.76 s): the 16 private copies of the payoff sums
+# workload, from a one-pass Nsight Compute capture of the full batch (30.83 MB
+# read, 0 written, 5.41 s): the 16 private copies of the payoff sums
 # (11.1 MB) and the descriptors the launch reads (19.7 MB, most of them the
 # 1.0M tiles), against 19.9 MB of algorithmic bytes (descriptors and results).
-PATHS_KERNEL_DRAM_BYTES = 30.69e6
+PATHS_KERNEL_DRAM_BYTES = 30.83e6
 PATHS_KERNEL_DRAM_NOTE = ("DRAM bytes per launch of the full batch, one-pass ncu capture: the 16 private copies "
                           "of the sums and the descriptors; algorithmic bytes 19.9 MB")
 
