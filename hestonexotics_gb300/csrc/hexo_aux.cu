@@ -146,19 +146,36 @@ __global__ void dbg_normals_kernel(const uint64_t *words, uint64_t n, double *ou
     }
 }
 
-// Every float bit pattern b in [lo, hi) through AS241's central branch
-// (branch 0, Q = b) or its tail (branch 1, R = b), once with the kernels'
-// division and root and once with the IEEE intrinsics: counts the results
-// whose bits differ and keeps the smallest such pattern.
+// Branches 0 and 1: every float bit pattern b in [lo, hi) through AS241's
+// central branch (Q = b) or its tail (R = b), once with the kernels' division
+// and root and once with the IEEE intrinsics.  Branch 2: every high word
+// b in [lo, hi) of a raw word, with low words at both ends of the range the
+// 32-bit input stage accepts (0x800 and 2^32 - 0x801), at 2^31 and at a hash
+// of b: where that stage certifies Q, it must equal the exact stage's Q on
+// the central branch.  Counts the disagreements and keeps the smallest b.
 __global__ void dbg_as241_check_kernel(uint32_t branch, uint64_t lo, uint64_t hi, unsigned long long *out) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long bad = 0;
     uint32_t first = 0xffffffffu;
     for (uint64_t b = lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < hi; b += stride) {
-        const float x = __uint_as_float((uint32_t)b);
-        const float f = branch == 0u ? dev::as241_central<false>(x) : dev::as241_tail<false>(x, false);
-        const float r = branch == 0u ? dev::as241_central<true>(x) : dev::as241_tail<true>(x, false);
-        if (__float_as_uint(f) != __float_as_uint(r)) {
+        bool differ = false;
+        if (branch == 2u) {
+            const uint32_t lows[4] = {0x800u, 0xfffff7ffu, 0x80000000u, (uint32_t)b * 2654435761u ^ 0x5bd1e995u};
+            for (int k = 0; k < 4; ++k) {
+                const uint64_t w = (b << 32) | lows[k];
+                float q;
+                if (dev::as241_fast_q(w, q)) {
+                    const dev::As241In ex = dev::as241_prep(w);
+                    differ |= !ex.central || __float_as_uint(q) != __float_as_uint(ex.q);
+                }
+            }
+        } else {
+            const float x = __uint_as_float((uint32_t)b);
+            const float f = branch == 0u ? dev::as241_central<false>(x) : dev::as241_tail<false>(x, false);
+            const float r = branch == 0u ? dev::as241_central<true>(x) : dev::as241_tail<true>(x, false);
+            differ = __float_as_uint(f) != __float_as_uint(r);
+        }
+        if (differ) {
             ++bad;
             first = min(first, (uint32_t)b);
         }

@@ -737,7 +737,7 @@ hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n,
 
 hexo_status hexo_debug_as241_check(hexo_ctx *ctx, uint32_t branch, uint64_t bits_lo, uint64_t bits_hi,
                                    uint64_t *out2) {
-    if (!ctx || !out2 || branch > 1u || bits_hi > (1ull << 32) || bits_lo > bits_hi) return HEXO_ERR_INVALID;
+    if (!ctx || !out2 || branch > 2u || bits_hi > (1ull << 32) || bits_lo > bits_hi) return HEXO_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->run_mu);
     cudaSetDevice(ctx->device);
     DevBuf dout;

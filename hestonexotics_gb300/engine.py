@@ -469,8 +469,9 @@ class Engine:
 
     def as241_check(self, branch: int, bits_lo: int, bits_hi: int) -> tuple[int, int]:
         """Float bit patterns in [bits_lo, bits_hi) through AS241's central branch (0) or tail (1) with the
-        kernels' division and root and with the IEEE intrinsics: (number of differing results, smallest
-        differing pattern or 2^64 - 1)."""
+        kernels' division and root and with the IEEE intrinsics, or (2) raw words with high words in
+        [bits_lo, bits_hi) through the 32-bit input stage and the exact one: (number of disagreements,
+        smallest disagreeing b or 2^64 - 1)."""
         out = np.zeros(2, dtype=np.uint64)
         self._check(self._lib.hexo_debug_as241_check(self._ctx, branch, bits_lo, bits_hi, _u64p(out)))
         return int(out[0]), int(out[1])

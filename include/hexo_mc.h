@@ -480,15 +480,18 @@ hexo_status hexo_debug_rng_draws(hexo_ctx *ctx, uint32_t seed, uint32_t stream, 
                                  const uint8_t *kinds, uint32_t n, double *out);
 /* AS241 of u = (double)w / (double)UINT64_MAX for each word: out[i]. */
 hexo_status hexo_debug_normals(hexo_ctx *ctx, const uint64_t *words, uint64_t n, double *out);
-/* Checks the division and square root that the path kernels use inside
- * AS241 (a reciprocal estimate with Newton and Markstein corrections, in
- * place of the IEEE intrinsics) on a range of inputs: every float bit
- * pattern b in [bits_lo, bits_hi), bits_hi <= 2^32, goes through AS241's
- * central branch (branch 0, Q = b) or its tail (branch 1, R = b) once each
- * way.  out2[0] receives how many results differ in any bit and out2[1] the
- * smallest such pattern (UINT64_MAX when none).  No reference counterpart:
- * it pins the kernels' arithmetic to the reference's IEEE float AS241
- * (src/as241.f90:88-116). */
+/* Checks the path kernels' shortcuts inside AS241 on a range of inputs,
+ * b in [bits_lo, bits_hi) with bits_hi <= 2^32.  Branches 0 and 1: the
+ * division and square root (a reciprocal estimate with Newton and Markstein
+ * corrections, in place of the IEEE intrinsics); every float bit pattern b
+ * goes through the central branch (branch 0, Q = b) or the tail (branch 1,
+ * R = b) once each way.  Branch 2: the 32-bit input stage; for every high
+ * word b of a raw word, with low words 0x800, 2^32 - 0x801, 2^31 and a hash
+ * of b, a Q the 32-bit stage certifies must equal the exact stage's.
+ * out2[0] receives how many b disagree and out2[1] the smallest such b
+ * (UINT64_MAX when none).  No reference counterpart: it pins the kernels'
+ * arithmetic to the reference's float AS241 on the double uniform
+ * (src/as241.f90:86-116, src/RNG.cpp:34-43). */
 hexo_status hexo_debug_as241_check(hexo_ctx *ctx, uint32_t branch, uint64_t bits_lo, uint64_t bits_hi,
                                    uint64_t *out2);
 /* The fixed-point split of payoffs as the path kernels fold them for a

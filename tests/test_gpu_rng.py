@@ -122,6 +122,13 @@ def test_as241_division_and_root_on_every_input(engine):
     assert engine.as241_check(1, F32_2M64, F32_HALF + 1) == none
 
 
+def test_as241_32bit_stage_on_every_high_word(engine):
+    """The conversion certifies most words' Q in 32-bit arithmetic (2|s| +- 1 converted once, s the high
+    word less 2^31); for all 2^32 high words, with low words at both ends of the accepted range, at 2^31
+    and hashed, every certified Q must equal the exact stage's (the reference's double arithmetic)."""
+    assert engine.as241_check(2, 0, 2 ** 32) == (0, 2 ** 64 - 1)
+
+
 def test_draw_moments_across_streams(engine):
     # moments of the per-path streams the kernels use (RNG(16, seed + k)),
     # 4096 streams x 2048 draws of each kind, within 5 standard errors;
