@@ -33,6 +33,12 @@ namespace {
 constexpr int kCvNodesNear = 256, kCvNodesTail = 128;
 constexpr int kCvNodes = kCvNodesNear + kCvNodesTail;
 constexpr double kCvRange = 40.0;
+// A parameter set with at most this many control-variate maturities runs
+// their recursions one warp per (maturity, node) (cv_cf_warp_kernel): alone,
+// its few thousand pairs could not fill the GPU one thread each.  The choice
+// depends on the set only, never on the batch around it, so a request's
+// prices stay the same bits in any batch.
+constexpr uint32_t kCvWarpMats = 32;
 
 struct CvMat {                     // one (set, maturity) with control-variate options
     uint32_t step_begin, n_steps;  // its grid steps: (dt, c) in the step array
@@ -88,10 +94,11 @@ __device__ __forceinline__ void heston_affine(cd a, cd b, double tau, const CvMa
 
 // phi[m * (kCvNodes + 1) + i] = E[exp(z L)], z = 1/2 + i U x_i for the nodes
 // and z = 1 (E[G] / S0) at i = kCvNodes.
-__global__ void cv_cf_kernel(const CvMat *__restrict__ mats, uint32_t n_mats, const double2 *__restrict__ steps,
-                             const double2 *__restrict__ nodes, double2 *__restrict__ phi) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_mats * (uint32_t)(kCvNodes + 1)) return;
+__global__ void cv_cf_kernel(const CvMat *__restrict__ mats, uint32_t mat0, uint32_t n_mats,
+                             const double2 *__restrict__ steps, const double2 *__restrict__ nodes,
+                             double2 *__restrict__ phi) {
+    const uint32_t t = mat0 * (kCvNodes + 1) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (mat0 + n_mats) * (uint32_t)(kCvNodes + 1)) return;
     const uint32_t mi = t / (kCvNodes + 1), i = t % (kCvNodes + 1);
     const CvMat m = mats[mi];
     const cd z = i == (uint32_t)kCvNodes ? cd{1.0, 0.0} : cd{0.5, m.U * nodes[i].x};
@@ -108,26 +115,130 @@ __global__ void cv_cf_kernel(const CvMat *__restrict__ mats, uint32_t n_mats, co
     phi[t] = make_double2(r.x, r.y);
 }
 
-// eg[out] = E[(G - K)^+] (undiscounted) for each control-variate option.
+// The same recursion for one (maturity, node) per warp, for requests too
+// small to fill the GPU with one thread per pair (each SM's FP64 pipe then
+// serves a single warp that walks every grid step in turn).  Over a fixed
+// step, heston_affine's B is a Moebius map of the terminal exponent b:
+//   B(b) = (M00 b + M01) / (M10 b + M11),  e = exp(-D tau),
+//   M = [[(beta + D) e - (beta - D), a (a - 1) (1 - e)], [s2 (e - 1), (beta + D) - (beta - D) e]]
+// ((beta - D)(beta + D) = s2 a (a - 1) by the definition of D).  Lane l
+// takes a block of consecutive steps; one warp scan gives every block the
+// sum of the c_j after it and the product of the later blocks' maps, whose
+// value at b = 0 is the b entering the block's last step; the lane then runs
+// heston_affine backward over its own steps, exactly as the one-thread
+// kernel does, and the warp sums the A terms.
+__device__ __forceinline__ void mobius(cd a, double tau, const CvMat &m, cd (&M)[4]) {
+    const double s2 = m.sigma * m.sigma;
+    const cd beta = {m.kappa - m.rho * m.sigma * a.x, -m.rho * m.sigma * a.y};
+    const cd aam1 = cmul(a, cd{a.x - 1.0, a.y});
+    cd D = csqrt(csub(cmul(beta, beta), cscale(aam1, s2)));
+    if (D.x < 0.0) D = {-D.x, -D.y};
+    const cd e = cexp(cscale(D, -tau));
+    const cd bpd = cadd(beta, D), bmd = csub(beta, D);
+    M[0] = csub(cmul(bpd, e), bmd);
+    M[1] = cmul(aam1, cd{1.0 - e.x, -e.y});
+    M[2] = cscale(cd{e.x - 1.0, e.y}, s2);
+    M[3] = csub(bpd, cmul(bmd, e));
+}
+// X <- X Y, rescaled by a power of two (a Moebius map does not change when
+// its matrix is scaled, and the products of many steps would otherwise
+// drift out of range).
+__device__ __forceinline__ void mobius_mul(cd (&X)[4], const cd (&Y)[4]) {
+    cd R[4];
+    R[0] = cadd(cmul(X[0], Y[0]), cmul(X[1], Y[2]));
+    R[1] = cadd(cmul(X[0], Y[1]), cmul(X[1], Y[3]));
+    R[2] = cadd(cmul(X[2], Y[0]), cmul(X[3], Y[2]));
+    R[3] = cadd(cmul(X[2], Y[1]), cmul(X[3], Y[3]));
+    double mx = 0.0;
+    for (int i = 0; i < 4; ++i) mx = fmax(mx, fmax(fabs(R[i].x), fabs(R[i].y)));
+    const int ex = mx > 0.0 ? ilogb(mx) : 0;
+    for (int i = 0; i < 4; ++i) X[i] = {scalbn(R[i].x, -ex), scalbn(R[i].y, -ex)};
+}
+__device__ __forceinline__ cd shfl_down_cd(cd v, unsigned d) {
+    return {__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d)};
+}
+
+__global__ void cv_cf_warp_kernel(const CvMat *__restrict__ mats, uint32_t n_mats, const double2 *__restrict__ steps,
+                                  const double2 *__restrict__ nodes, double2 *__restrict__ phi) {
+    const uint32_t t = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31u;
+    if (t >= n_mats * (uint32_t)(kCvNodes + 1)) return;   // warp-uniform
+    const uint32_t mi = t / (kCvNodes + 1), i = t % (kCvNodes + 1);
+    const CvMat m = mats[mi];
+    const cd z = i == (uint32_t)kCvNodes ? cd{1.0, 0.0} : cd{0.5, m.U * nodes[i].x};
+    const uint32_t per = (m.n_steps + 31u) / 32u, k0 = min(lane * per, m.n_steps), k1 = min(k0 + per, m.n_steps);
+    const double2 *st = steps + m.step_begin;
+    // the block's own sum of c and product of maps (steps k0 .. k1 - 1, applied last to first)
+    double csum = 0.0;
+    for (uint32_t k = k0; k < k1; ++k) csum += st[k].y;
+    // c after the block: an exclusive suffix sum over the lanes
+    double cs = csum;
+    for (unsigned d = 1; d < 32u; d <<= 1) {
+        const double x = __shfl_down_sync(0xffffffffu, cs, d);
+        if (lane + d < 32u) cs += x;
+    }
+    double c_after = __shfl_down_sync(0xffffffffu, cs, 1);
+    if (lane == 31u) c_after = 0.0;
+    cd P[4] = {{1.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}, {1.0, 0.0}};
+    {
+        double C = c_after;
+        cd Mk[4];
+        for (uint32_t k = k1; k-- > k0;) {   // P = M_k0 ... M_(k1-1)
+            C += st[k].y;
+            mobius(cscale(z, C), st[k].x, m, Mk);
+            cd T[4] = {Mk[0], Mk[1], Mk[2], Mk[3]};
+            mobius_mul(T, P);
+            for (int q = 0; q < 4; ++q) P[q] = T[q];
+        }
+    }
+    // the later blocks' maps: an inclusive suffix product, then shifted by one lane
+    cd S[4] = {P[0], P[1], P[2], P[3]};
+    for (unsigned d = 1; d < 32u; d <<= 1) {
+        cd X[4];
+        for (int q = 0; q < 4; ++q) X[q] = shfl_down_cd(S[q], d);
+        if (lane + d < 32u) mobius_mul(S, X);
+    }
+    cd N[4];
+    for (int q = 0; q < 4; ++q) N[q] = shfl_down_cd(S[q], 1);
+    cd b = lane == 31u ? cd{0.0, 0.0} : cdiv(N[1], N[3]);   // the later blocks' map at b = 0
+    // this block's steps, backward, as the one-thread recursion runs them
+    cd Asum = {0.0, 0.0};
+    double C = c_after;
+    for (uint32_t k = k1; k-- > k0;) {
+        C += st[k].y;
+        cd A, B;
+        heston_affine(cscale(z, C), b, st[k].x, m, A, B);
+        Asum = cadd(Asum, A);
+        b = B;
+    }
+    for (unsigned d = 16; d > 0u; d >>= 1) Asum = cadd(Asum, shfl_down_cd(Asum, d));
+    if (lane == 0u) {   // lane 0's block is the first: its b is b_0
+        const cd r = cexp(cadd(Asum, cscale(b, m.v0)));
+        phi[t] = make_double2(r.x, r.y);
+    }
+}
+
+// eg[out] = E[(G - K)^+] (undiscounted) for each control-variate option:
+// one warp per option, its lanes over the quadrature nodes.
 __global__ void cv_price_kernel(const CvMat *__restrict__ mats, const CvOpt *__restrict__ opts, uint32_t n_opts,
                                 const double2 *__restrict__ nodes, const double2 *__restrict__ phi,
                                 double *__restrict__ eg) {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_opts) return;
+    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (q >= n_opts) return;   // warp-uniform
     const CvOpt o = opts[q];
     const CvMat m = mats[o.mat];
     const double2 *ph = phi + (size_t)o.mat * (kCvNodes + 1);
     const double F = m.S0 * ph[kCvNodes].x;
     const double lf = log(F / m.S0), k = log(F / o.K);
     double sum = 0.0;
-    for (int i = 0; i < kCvNodes; ++i) {
+    for (int i = (int)lane; i < kCvNodes; i += 32) {
         const double u = m.U * nodes[i].x, w = m.U * nodes[i].y;
         const cd z = {0.5, u};
         const cd psi = cmul(cd{ph[i].x, ph[i].y}, cexp(cscale(z, -lf)));
         const cd ek = cexp(cd{0.0, u * k});
         sum += w * cmul(ek, psi).x / (u * u + 0.25);
     }
-    eg[o.out] = F - sqrt(F * o.K) / M_PI * sum;
+    for (unsigned d = 16; d > 0u; d >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, d);
+    if (lane == 0u) eg[o.out] = F - sqrt(F * o.K) / M_PI * sum;
 }
 
 // Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_N).
@@ -230,7 +341,20 @@ cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32
     std::vector<CvOpt> opts;
     std::vector<double2> steps;
     std::map<std::pair<uint32_t, uint32_t>, uint32_t> mat_of;
-    for (const BatchPlan::CvLeader &l : bp.cv) {
+    // sets with few control-variate maturities first: their recursions run one warp per pair
+    std::map<uint32_t, uint32_t> n_mats_of_set;
+    {
+        std::map<std::pair<uint32_t, uint32_t>, bool> seen;
+        for (const BatchPlan::CvLeader &l : bp.cv)
+            if (seen.emplace(std::make_pair(l.set, l.mat), true).second) ++n_mats_of_set[l.set];
+    }
+    std::vector<const BatchPlan::CvLeader *> order;
+    for (int pass = 0; pass < 2; ++pass)
+        for (const BatchPlan::CvLeader &l : bp.cv)
+            if ((n_mats_of_set[l.set] <= kCvWarpMats) == (pass == 0)) order.push_back(&l);
+    uint32_t n_warp_mats = 0;
+    for (const BatchPlan::CvLeader *lp : order) {
+        const BatchPlan::CvLeader &l = *lp;
         h_partner[l.leader] = l.gslot;
         const auto key = std::make_pair(l.set, l.mat);
         auto it = mat_of.find(key);
@@ -245,6 +369,7 @@ cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32
             m.S0 = bp.sets[l.set].S0;
             it = mat_of.emplace(key, (uint32_t)mats.size()).first;
             mats.push_back(m);
+            if (n_mats_of_set[l.set] <= kCvWarpMats) ++n_warp_mats;
         }
         opts.push_back(CvOpt{it->second, l.leader, l.strike});
     }
@@ -260,16 +385,26 @@ cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32
         if (e == cudaSuccess) e = upload(steps, d_steps, st);
         if (e == cudaSuccess) e = upload(nodes, d_nodes, st);
         if (e == cudaSuccess) e = cudaMalloc(&d_phi, mats.size() * (kCvNodes + 1) * sizeof(double2));
-        if (e == cudaSuccess) {
-            // one warp per block: a single request's few hundred threads spread over as many SMs
-            // as possible (the recursion is bound by each SM's FP64 pipe)
-            const uint32_t n_thr = (uint32_t)mats.size() * (kCvNodes + 1);
-            cv_cf_kernel<<<(n_thr + 31) / 32, 32, 0, st>>>(d_mats, (uint32_t)mats.size(), d_steps, d_nodes, d_phi);
+        // the recursion is bound by each SM's FP64 pipe: sets with few maturities one warp per
+        // (maturity, node) over the steps (about 1.5 times the arithmetic, over 32 lanes), the
+        // rest one thread per pair, one warp per block so that the pairs spread over the SMs
+        if (e == cudaSuccess && n_warp_mats > 0) {
+            const uint64_t n_thr = (uint64_t)n_warp_mats * (kCvNodes + 1) * 32u;
+            cv_cf_warp_kernel<<<(unsigned)((n_thr + 63) / 64), 64, 0, st>>>(d_mats, n_warp_mats, d_steps, d_nodes,
+                                                                           d_phi);
+            e = cudaGetLastError();
+        }
+        const uint32_t n_thread_mats = (uint32_t)mats.size() - n_warp_mats;
+        if (e == cudaSuccess && n_thread_mats > 0) {
+            const uint32_t n_pairs = n_thread_mats * (kCvNodes + 1);
+            cv_cf_kernel<<<(n_pairs + 31) / 32, 32, 0, st>>>(d_mats, n_warp_mats, n_thread_mats, d_steps, d_nodes,
+                                                             d_phi);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
-            cv_price_kernel<<<((uint32_t)opts.size() + 127) / 128, 128, 0, st>>>(d_mats, d_opts, (uint32_t)opts.size(),
-                                                                                  d_nodes, d_phi, *eg);
+            const uint64_t n_thr = (uint64_t)opts.size() * 32u;
+            cv_price_kernel<<<(unsigned)((n_thr + 127) / 128), 128, 0, st>>>(d_mats, d_opts, (uint32_t)opts.size(),
+                                                                             d_nodes, d_phi, *eg);
             e = cudaGetLastError();
         }
     }

@@ -38,6 +38,20 @@ def test_fp64_control_variate_equals_oracle(engine, oracle, maker):
     np.testing.assert_allclose(se, ose, rtol=1e-6, atol=1e-12 * req.S0)
 
 
+def test_fp64_control_variate_many_maturities_equals_oracle(engine, oracle):
+    """A set with more control-variate maturities than the warp-per-pair recursion takes (32) runs the
+    one-thread-per-(maturity, node) recursion; short maturities keep the oracle's recursion quick."""
+    req, cfg = W.single_chain(n_paths=1 << 12)
+    T = np.arange(1, 41) * 5 / 252.0                       # 40 maturities, 5 to 200 trading days
+    req.options = E.Options(strike=np.full(40, req.S0), T=T, payoff=E.ASIAN)
+    cfg.precision = E.FP64
+    cfg.control_variate = 1
+    p, se = engine.price(req.params, req.S0, req.options, cfg)
+    op, ose = oracle_cv(oracle, req, cfg)
+    np.testing.assert_allclose(p, op, rtol=1e-8, atol=1e-9 * req.S0)
+    np.testing.assert_allclose(se, ose, rtol=1e-6, atol=1e-12 * req.S0)
+
+
 def test_control_variate_against_the_plain_estimator(engine):
     req, cfg = W.single_chain(n_paths=1 << 16, precision=E.FP32)
     p, se = engine.price(req.params, req.S0, req.options, cfg)
