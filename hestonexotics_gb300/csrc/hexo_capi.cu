@@ -94,8 +94,6 @@ DeviceBatch::~DeviceBatch() {
     if (ev_k1) cudaEventDestroy(ev_k1);
     if (dmem && own_d) cudaFree(dmem);
     if (hmem && own_h) cudaFreeHost(hmem);
-    if (d_cv_eg) cudaFree(d_cv_eg);
-    if (d_cv_partner) cudaFree(d_cv_partner);
 }
 
 namespace {
@@ -130,6 +128,9 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
     const size_t o_price = take(n_out * sizeof(double));
     const size_t o_se = take(n_out * sizeof(double));
     const size_t o_ctl = take(kCtlBytes);   // queue head, error flags, exponential-branch steps
+    CvPlan cvp;                              // the control variate's analytic part (host vectors until the sync)
+    if (!bp.cv.empty()) cv_plan(bp, cvp);
+    const size_t o_cv = take(cvp.bytes);
     db.bytes = off;
     cudaError_t e = cudaSuccess;
     if (db.dmem == nullptr || db.dcap < db.bytes) {
@@ -202,6 +203,10 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
         (e = up(o_pexp, bp.opt_pexp.data(), n_out * sizeof(int32_t))) != cudaSuccess ||
         (carried && (e = up(o_carry, bp.opt_carry.data(), n_out * sizeof(uint64_t))) != cudaSuccess))
         return cuda_fail(ctx, e, "upload batch");
+    db.d_cv_eg = nullptr;
+    db.d_cv_partner = nullptr;
+    if (!bp.cv.empty() && (e = cv_run(cvp, d + o_cv, st, &db.d_cv_eg, &db.d_cv_partner)) != cudaSuccess)
+        return cuda_fail(ctx, e, "control variate");
     e = cudaStreamSynchronize(st);   // the host vectors are pageable: finish before they can change
     if (e != cudaSuccess) return cuda_fail(ctx, e, "upload batch");
     db.h2d_bytes = bp.sets.size() * sizeof(SetDesc) + bp.segs.size() * sizeof(SegDesc) +
@@ -209,8 +214,6 @@ hexo_status batch_upload(hexo_ctx *ctx, BatchPlan &&plan, bool f32, DeviceBatch 
                    bp.tiles.size() * sizeof(TileDesc) + n_out * (sizeof(uint64_t) + sizeof(double) + sizeof(int32_t));
     if ((e = cudaEventCreate(&db.ev_k0)) != cudaSuccess || (e = cudaEventCreate(&db.ev_k1)) != cudaSuccess)
         return cuda_fail(ctx, e, "cudaEventCreate");
-    if (!bp.cv.empty() && (e = cv_prepare(bp, st, &db.d_cv_eg, &db.d_cv_partner)) != cudaSuccess)
-        return cuda_fail(ctx, e, "control variate");
     return HEXO_OK;
 }
 

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <vector>
 #include "hexo_plan.h"
@@ -320,26 +321,16 @@ void cv_schedule(const BatchPlan &bp, uint32_t s, uint32_t j, std::vector<double
     for (size_t k = 0; k < n; ++k) out.push_back(make_double2(dts[k], c[k]));
 }
 
-template <class T>
-cudaError_t upload(const std::vector<T> &v, T *&d, cudaStream_t st) {
-    cudaError_t e = cudaMalloc(&d, std::max<size_t>(1, v.size()) * sizeof(T));
-    if (e == cudaSuccess && !v.empty()) e = cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
-    return e;
-}
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 } // namespace
 
-// Computes E[(G - K)^+] of every control-variate option into eg (indexed by
-// output slot, NaN elsewhere) and the slot of its geometric sums into partner
-// (~0 elsewhere).  Both device arrays have n_out entries; allocated here.
-cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32_t **partner) {
-    *eg = nullptr;
-    *partner = nullptr;
-    std::vector<double> h_eg(bp.n_out, std::nan(""));
-    std::vector<uint32_t> h_partner(bp.n_out, ~0u);
+void cv_plan(const BatchPlan &bp, CvPlan &cp) {
+    cp = CvPlan{};
+    cp.eg.assign(bp.n_out, std::nan(""));
+    cp.partner.assign(bp.n_out, ~0u);
     std::vector<CvMat> mats;
     std::vector<CvOpt> opts;
-    std::vector<double2> steps;
     std::map<std::pair<uint32_t, uint32_t>, uint32_t> mat_of;
     // sets with few control-variate maturities first: their recursions run one warp per pair
     std::map<uint32_t, uint32_t> n_mats_of_set;
@@ -352,69 +343,82 @@ cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32
     for (int pass = 0; pass < 2; ++pass)
         for (const BatchPlan::CvLeader &l : bp.cv)
             if ((n_mats_of_set[l.set] <= kCvWarpMats) == (pass == 0)) order.push_back(&l);
-    uint32_t n_warp_mats = 0;
     for (const BatchPlan::CvLeader *lp : order) {
         const BatchPlan::CvLeader &l = *lp;
-        h_partner[l.leader] = l.gslot;
+        cp.partner[l.leader] = l.gslot;
         const auto key = std::make_pair(l.set, l.mat);
         auto it = mat_of.find(key);
         if (it == mat_of.end()) {
             CvMat m{};
-            m.step_begin = (uint32_t)steps.size();
-            cv_schedule(bp, l.set, l.mat, steps, m.U);
-            m.n_steps = (uint32_t)steps.size() - m.step_begin;
+            m.step_begin = (uint32_t)cp.steps.size();
+            cv_schedule(bp, l.set, l.mat, cp.steps, m.U);
+            m.n_steps = (uint32_t)cp.steps.size() - m.step_begin;
             const hexo_params &p = bp.set_params[l.set];
             m.v0 = p.v0; m.kappa = p.kappa; m.theta = p.theta; m.sigma = p.sigma; m.rho = p.rho;
             m.mu = p.r - p.q;
             m.S0 = bp.sets[l.set].S0;
             it = mat_of.emplace(key, (uint32_t)mats.size()).first;
             mats.push_back(m);
-            if (n_mats_of_set[l.set] <= kCvWarpMats) ++n_warp_mats;
+            if (n_mats_of_set[l.set] <= kCvWarpMats) ++cp.n_warp_mats;
         }
         opts.push_back(CvOpt{it->second, l.leader, l.strike});
     }
-    const std::vector<double2> nodes = unit_nodes();
-    CvMat *d_mats = nullptr;
-    CvOpt *d_opts = nullptr;
-    double2 *d_steps = nullptr, *d_nodes = nullptr, *d_phi = nullptr;
-    cudaError_t e = upload(h_eg, *eg, st);
-    if (e == cudaSuccess) e = upload(h_partner, *partner, st);
-    if (e == cudaSuccess && !mats.empty()) {
-        if (e == cudaSuccess) e = upload(mats, d_mats, st);
-        if (e == cudaSuccess) e = upload(opts, d_opts, st);
-        if (e == cudaSuccess) e = upload(steps, d_steps, st);
-        if (e == cudaSuccess) e = upload(nodes, d_nodes, st);
-        if (e == cudaSuccess) e = cudaMalloc(&d_phi, mats.size() * (kCvNodes + 1) * sizeof(double2));
-        // the recursion is bound by each SM's FP64 pipe: sets with few maturities one warp per
-        // (maturity, node) over the steps (about 1.5 times the arithmetic, over 32 lanes), the
-        // rest one thread per pair, one warp per block so that the pairs spread over the SMs
-        if (e == cudaSuccess && n_warp_mats > 0) {
-            const uint64_t n_thr = (uint64_t)n_warp_mats * (kCvNodes + 1) * 32u;
-            cv_cf_warp_kernel<<<(unsigned)((n_thr + 63) / 64), 64, 0, st>>>(d_mats, n_warp_mats, d_steps, d_nodes,
-                                                                           d_phi);
-            e = cudaGetLastError();
-        }
-        const uint32_t n_thread_mats = (uint32_t)mats.size() - n_warp_mats;
-        if (e == cudaSuccess && n_thread_mats > 0) {
-            const uint32_t n_pairs = n_thread_mats * (kCvNodes + 1);
-            cv_cf_kernel<<<(n_pairs + 31) / 32, 32, 0, st>>>(d_mats, n_warp_mats, n_thread_mats, d_steps, d_nodes,
-                                                             d_phi);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) {
-            const uint64_t n_thr = (uint64_t)opts.size() * 32u;
-            cv_price_kernel<<<(unsigned)((n_thr + 127) / 128), 128, 0, st>>>(d_mats, d_opts, (uint32_t)opts.size(),
-                                                                             d_nodes, d_phi, *eg);
-            e = cudaGetLastError();
-        }
+    static const std::vector<double2> kNodes = unit_nodes();   // the same nodes for every batch
+    cp.nodes = kNodes;
+    cp.n_mats = (uint32_t)mats.size();
+    cp.n_opts = (uint32_t)opts.size();
+    cp.mats.resize(mats.size() * sizeof(CvMat));
+    if (!mats.empty()) std::memcpy(cp.mats.data(), mats.data(), cp.mats.size());
+    cp.opts.resize(opts.size() * sizeof(CvOpt));
+    if (!opts.empty()) std::memcpy(cp.opts.data(), opts.data(), cp.opts.size());
+    cp.bytes = align256(cp.eg.size() * sizeof(double)) + align256(cp.partner.size() * sizeof(uint32_t)) +
+               align256(cp.mats.size()) + align256(cp.opts.size()) + align256(cp.steps.size() * sizeof(double2)) +
+               align256(cp.nodes.size() * sizeof(double2)) +
+               align256((size_t)cp.n_mats * (kCvNodes + 1) * sizeof(double2));
+}
+
+cudaError_t cv_run(const CvPlan &cp, void *region, cudaStream_t st, double **eg, uint32_t **partner) {
+    char *d = static_cast<char *>(region);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = d + off; off += align256(bytes); return p; };
+    double *d_eg = reinterpret_cast<double *>(take(cp.eg.size() * sizeof(double)));
+    uint32_t *d_partner = reinterpret_cast<uint32_t *>(take(cp.partner.size() * sizeof(uint32_t)));
+    CvMat *d_mats = reinterpret_cast<CvMat *>(take(cp.mats.size()));
+    CvOpt *d_opts = reinterpret_cast<CvOpt *>(take(cp.opts.size()));
+    double2 *d_steps = reinterpret_cast<double2 *>(take(cp.steps.size() * sizeof(double2)));
+    double2 *d_nodes = reinterpret_cast<double2 *>(take(cp.nodes.size() * sizeof(double2)));
+    double2 *d_phi = reinterpret_cast<double2 *>(take((size_t)cp.n_mats * (kCvNodes + 1) * sizeof(double2)));
+    *eg = d_eg;
+    *partner = d_partner;
+    auto up = [&](void *dst, const void *src, size_t bytes) -> cudaError_t {
+        return bytes == 0 ? cudaSuccess : cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    cudaError_t e = up(d_eg, cp.eg.data(), cp.eg.size() * sizeof(double));
+    if (e == cudaSuccess) e = up(d_partner, cp.partner.data(), cp.partner.size() * sizeof(uint32_t));
+    if (e == cudaSuccess) e = up(d_mats, cp.mats.data(), cp.mats.size());
+    if (e == cudaSuccess) e = up(d_opts, cp.opts.data(), cp.opts.size());
+    if (e == cudaSuccess) e = up(d_steps, cp.steps.data(), cp.steps.size() * sizeof(double2));
+    if (e == cudaSuccess) e = up(d_nodes, cp.nodes.data(), cp.nodes.size() * sizeof(double2));
+    if (e != cudaSuccess || cp.n_mats == 0) return e;
+    // the recursion is bound by each SM's FP64 pipe: sets with few maturities one warp per
+    // (maturity, node) over the steps (about 1.5 times the arithmetic, over 32 lanes), the
+    // rest one thread per pair, one warp per block so that the pairs spread over the SMs
+    if (cp.n_warp_mats > 0) {
+        const uint64_t n_thr = (uint64_t)cp.n_warp_mats * (kCvNodes + 1) * 32u;
+        cv_cf_warp_kernel<<<(unsigned)((n_thr + 63) / 64), 64, 0, st>>>(d_mats, cp.n_warp_mats, d_steps, d_nodes,
+                                                                       d_phi);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the host vectors go out of scope
-    cudaFree(d_mats);
-    cudaFree(d_opts);
-    cudaFree(d_steps);
-    cudaFree(d_nodes);
-    cudaFree(d_phi);
-    return e;
+    const uint32_t n_thread_mats = cp.n_mats - cp.n_warp_mats;
+    if (n_thread_mats > 0) {
+        const uint32_t n_pairs = n_thread_mats * (kCvNodes + 1);
+        cv_cf_kernel<<<(n_pairs + 31) / 32, 32, 0, st>>>(d_mats, cp.n_warp_mats, n_thread_mats, d_steps, d_nodes,
+                                                         d_phi);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const uint64_t n_thr = (uint64_t)cp.n_opts * 32u;
+    cv_price_kernel<<<(unsigned)((n_thr + 127) / 128), 128, 0, st>>>(d_mats, d_opts, cp.n_opts, d_nodes, d_phi, d_eg);
+    return cudaGetLastError();
 }
 
 } // namespace hexo

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <vector>
 #include "hexo_types.h"
 #include "hexo_plan.h"
 
@@ -51,9 +52,24 @@ struct FinalizeArgs {
 };
 cudaError_t launch_finalize(const FinalizeArgs &f, cudaStream_t st);
 // The geometric control variate's analytic part for a planned batch:
-// E[(G - K)^+] per control-variate option into *eg and its geometric-sum slot
-// into *partner (device arrays of n_out entries, allocated here).
-cudaError_t cv_prepare(const BatchPlan &bp, cudaStream_t st, double **eg, uint32_t **partner);
+// The control variate's analytic part, in two halves so that its device
+// memory is a region of the batch's arena (no allocation, so no device-wide
+// synchronisation, per batch).  cv_plan builds, on the host, what the
+// kernels need and the region's size; cv_run uploads it into `region` (256-byte
+// aligned, cv_plan's bytes long) on stream st and enqueues the kernels that
+// write E[(G - K)^+] per control-variate option into *eg and its geometric-sum
+// slot into *partner (arrays of n_out entries inside the region).  The plan's
+// host vectors must outlive the stream's copies.
+struct CvPlan {
+    std::vector<double> eg;          // n_out: NaN, filled on the device
+    std::vector<uint32_t> partner;   // n_out: ~0 except the control-variate options
+    std::vector<unsigned char> mats, opts;   // packed device records
+    std::vector<double2> steps, nodes;
+    uint32_t n_mats = 0, n_warp_mats = 0, n_opts = 0;
+    size_t bytes = 0;                // the device region
+};
+void cv_plan(const BatchPlan &bp, CvPlan &cp);
+cudaError_t cv_run(const CvPlan &cp, void *region, cudaStream_t st, double **eg, uint32_t **partner);
 
 // Debug kernels.
 cudaError_t launch_dbg_words(uint32_t seed, uint32_t stream, uint32_t n_streams, uint32_t n_words, uint64_t *out,

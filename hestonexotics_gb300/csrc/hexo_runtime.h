@@ -52,8 +52,8 @@ struct DeviceBatch {
     uint64_t *d_carry_row = nullptr;       // per output slot: (row << 1) | last block, ~0 = not carried
     double *h_price = nullptr, *h_se = nullptr;
     unsigned long long *h_acc = nullptr;
-    double *d_cv_eg = nullptr;         // control variate: E[(G - K)^+] per output slot (NaN elsewhere)
-    uint32_t *d_cv_partner = nullptr;  // control variate: the slot of the geometric sums (~0 elsewhere)
+    double *d_cv_eg = nullptr;         // control variate (in dmem): E[(G - K)^+] per output slot (NaN elsewhere)
+    uint32_t *d_cv_partner = nullptr;  // control variate (in dmem): the slot of the geometric sums (~0 elsewhere)
     uint32_t *h_ctl = nullptr;   // control block of the last run (kCtlBytes): queue head, error flags, quad steps
     cudaGraphExec_t graph_exec = nullptr;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around the path kernel

@@ -257,6 +257,11 @@ void admit(hexo_server *s) {
                 r->fixed_bytes = sizeof(SetDesc) + sp.segs.size() * sizeof(SegDesc) +
                                  sp.mats.size() * sizeof(MatDesc) + n_out * sizeof(OptDesc) +
                                  n_out * (kRowBytes * (kSumSlots + 1) + 48ull) + 4096;
+                // the control variate's region of the launch's arena, bounded with one maturity per
+                // option: per maturity its characteristic function at 385 nodes and its grid steps
+                if (sp.n_cv > 0)
+                    r->fixed_bytes += (uint64_t)sp.n_cv * (385ull * 16ull + r->deep_steps * 16ull + 64ull) +
+                                      n_out * 12ull + 384ull * 16ull + 7ull * 256ull;
                 // its smallest block (one tile; all of it with the control variate) beside the pool
                 if (block_bytes(s, *r, r->whole ? r->n_max : s->tile_paths) + s->pool_bytes > s->cap ||
                     (!r->whole && r->plan.n_user > s->pool.rows))
