@@ -657,7 +657,8 @@ def run_engine(args, rank, world, local):
             "scaling": "strong", "vs_baseline": None, "dtype": "f32 paths, f32 AS241, exact integer sums, f64 finalise",
             "data": "synthetic (seeded uneven 64-set batch; the reference prices live option chains)",
             "config": workload_config() if args.path_scale == 1.0 else
-            {**workload_config(), "workload": f"{WORKLOAD}_paths_x{args.path_scale:g}"},
+            {**workload_config(), "workload": f"{WORKLOAD}_paths_x{args.path_scale:g}",
+             "nominal_path_steps": int(nominal_batch)},
             "launch": {"form": "FP32, one persistent launch of the whole batch through a captured CUDA graph",
                        "paths": info["n_paths"], "executed_path_steps": info["executed_path_steps"],
                        "tiles": info["n_tiles"], "block": info["block"], "paths_per_thread": info["paths_per_thread"],
